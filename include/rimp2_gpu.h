@@ -1,0 +1,168 @@
+/*
+ * rimp2_gpu.h -- C-ABI of the GB300 (sm_103a) RI-MP2 amplitude / energy library.
+ *
+ * The entry points keep the argument lists of the CONTAINS subroutines of the
+ * reference program RIMP2.F90 (januseriksen/rimp2_gpu), so that the existing
+ * Fortran driver can call them through iso_c_binding interfaces without
+ * changing its arrays:
+ *   - integers arrive by reference (Fortran default), arrays are FP64
+ *     column-major with the reference's explicit shapes;
+ *   - array arguments are HOST pointers; the library copies in and out on its
+ *     own stream.  The *_dev variants take DEVICE pointers instead (the
+ *     `host_data use_device` idiom of RIMP2.GPU.F90:117,133,171,185,212,243)
+ *     and pass sizes by value;
+ *   - every entry returns an int status (RIMP2_OK = 0) and never stops the
+ *     process; rimp2_last_error_string() describes the last failure.  (The
+ *     reference discards every cuBLAS status, RIMP2.GPU.F90:81,119,135.)
+ * There is no CPU fallback: on a machine without a usable sm_103 GPU each
+ * compute entry returns RIMP2_ERR_NODEV.
+ */
+#ifndef RIMP2_GPU_H
+#define RIMP2_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RIMP2_OK 0
+#define RIMP2_ERR_ARG 1     /* invalid dimension or null pointer */
+#define RIMP2_ERR_CUDA 2    /* CUDA runtime / launch error */
+#define RIMP2_ERR_NOMEM 3   /* device allocation failed */
+#define RIMP2_ERR_NODEV 4   /* no usable GPU */
+#define RIMP2_ERR_TIMEOUT 5 /* a device-side bounded wait ran out */
+#define RIMP2_ERR_UNSUPPORTED 6
+
+#define RIMP2_PREC_FP64 0  /* plain FP64 (DMMA) fused kernel */
+#define RIMP2_PREC_SPLIT 1 /* split-precision tcgen05 alpha contraction */
+
+/* ---- library state ----------------------------------------------------- */
+/* Message of the last failing call on this thread ("" after success). */
+const char *rimp2_last_error_string(void);
+/* Library version string. */
+const char *rimp2_version(void);
+/* Route all work to a caller stream (cudaStream_t, NULL = library stream). */
+int rimp2_set_stream(void *stream);
+/* Total and free device memory.  Replaces get_dev_mem (cuda_api.cu:5-8,
+ * declared in gpu_interfaces.F90:47-53); pointer arguments instead of C++
+ * references so that C and Fortran bind(C) callers can use it. */
+int rimp2_get_dev_mem(size_t *total, size_t *free_bytes);
+/* Number of kernels this library has launched (all entry points). */
+long long rimp2_kernel_launch_count(void);
+
+/* ---- drop-in subroutines of RIMP2.F90 -----------------------------------
+ * Each replaces the subroutine cited beside it; argument names, order and
+ * array shapes are the reference's. */
+
+/* RIMP2_calc_toccA (RIMP2.F90:381-417; GPU form RIMP2.GPU.F90:475-517):
+ * tocc(i,jL,a,b) = sum_j [sum_al Calpha(al,a,i) Calpha(al,b,j) /
+ *                   (EVocc(i)+EVocc(j)-EVvirt(b)-EVvirt(a))] UoccEOST(j,jL) */
+int rimp2_calc_tocca(const int *nvirt, const int *nocc, const int *noccEOS, const int *NBA,
+                     const double *Calpha, const double *EVocc, const double *EVvirt,
+                     double *tocc, const double *UoccEOST);
+
+/* RIMP2_calc_tvirtA (RIMP2.F90:419-453; GPU RIMP2.GPU.F90:519-559):
+ * tvirt(i,j,aL,b) = sum_a [g/D](i,j,a,b) UvirtEOST(a,aL) */
+int rimp2_calc_tvirta(const int *nvirt, const int *nocc, const int *nvirtEOS, const int *NBA,
+                      const double *Calpha, const double *EVocc, const double *EVvirt,
+                      double *tvirt, const double *UvirtEOST);
+
+/* RIMP2_calc_toccB (RIMP2.F90:456-481; GPU RIMP2.GPU.F90:562-592):
+ * toccEOS(aL,iL,bL,jL) = sum_A tocc(iL,jL,A,bL) UvirtT(A,aL) */
+int rimp2_calc_toccb(const int *nvirt, const int *noccEOS, const double *tocc,
+                     const double *UvirtT, double *toccEOS);
+
+/* RIMP2_calc_tvirtB (RIMP2.F90:483-508; GPU RIMP2.GPU.F90:594-623):
+ * tvirtEOS(aL,iL,bL,jL) = sum_J tvirt(iL,J,aL,bL) UoccT(J,jL) */
+int rimp2_calc_tvirtb(const int *nvirtEOS, const int *nocc, const double *tvirt,
+                      const double *UoccT, double *tvirtEOS);
+
+/* RIMP2_TransAlpha1 (RIMP2.F90:510-533; GPU RIMP2.GPU.F90:625-650):
+ * AlphaCD5(al,bL,jL) = sum_B UvirtT(B,bL) AlphaCD4(al,B,jL) */
+int rimp2_transalpha1(const int *nvirt, const int *noccEOS, const int *nba, const double *UvirtT,
+                      const double *AlphaCD4, double *AlphaCD5);
+
+/* RIMP2_TransAlpha2 (RIMP2.F90:536-560; GPU RIMP2.GPU.F90:652-679):
+ * AlphaCD5(al,n3,n2) = sum_n1 U(n1,n3) AlphaCD4(al,n1,n2) */
+int rimp2_transalpha2(const int *n2, const int *n1, const int *n3, const int *nba,
+                      const double *U, const double *AlphaCD4, double *AlphaCD5);
+
+/* RIMP2_calc_gocc (RIMP2.F90:562-587; GPU RIMP2.GPU.F90:707-736):
+ * goccEOS(aL,iL,bL,jL) = sum_al Calpha3(al,aL,iL) Calpha3(al,bL,jL) */
+int rimp2_calc_gocc(const int *nvirt, const int *noccEOS, const int *NBA, const double *Calpha3,
+                    double *goccEOS);
+
+/* RIMP2_calc_gvirt (RIMP2.F90:589-614; GPU RIMP2.GPU.F90:738-766) */
+int rimp2_calc_gvirt(const int *nvirtEOS, const int *nocc, const int *NBA, const double *Calpha3,
+                     double *gvirtEOS);
+
+/* RIMP2_calc_gen4DimFO (RIMP2.F90:616-641; RIMP2.GPU.F90:768-793):
+ * djik(a,b,c,d) = sum_al Calpha3(al,a,b) Calpha4(al,c,d) */
+int rimp2_calc_gen4dimfo(const int *NBA, const double *Calpha3, const int *n1, const int *n2,
+                         const double *Calpha4, const int *n3, const int *n4, double *djik);
+
+/* Column-major DGEMM as called by the driver at RIMP2.F90:79,87,110,118,137,
+ * 160 (cublasDgemm_v2 at RIMP2.GPU.F90:119,135,172,186,213,244, bound in
+ * gpu_interfaces.F90:25-33).  transa/transb: 'N' or 'T'.  Hand-written FP64
+ * kernel, no cuBLAS. */
+int rimp2_dgemm(const char *transa, const char *transb, const int *m, const int *n, const int *k,
+                const double *alpha, const double *A, const int *lda, const double *B,
+                const int *ldb, const double *beta, double *C, const int *ldc);
+
+/* Driver Steps 5-8 in one call (RIMP2.F90:71-170 with first_order=.false.):
+ * toccEOS(nvirt,noccEOS,nvirt,noccEOS), tvirtEOS(nvirtEOS,nocc,nvirtEOS,nocc),
+ * goccEOS(nvirt,noccEOS,nvirt,noccEOS), gvirtEOS(nvirtEOS,nocc,nvirtEOS,nocc).
+ * All intermediates stay on the device. */
+int rimp2_steps5to8(const int *nvirt, const int *nocc, const int *noccEOS, const int *nvirtEOS,
+                    const int *NBA, const double *Calpha, const double *EVocc,
+                    const double *EVvirt, const double *UoccEOST, const double *UvirtT,
+                    const double *UoccT, const double *UvirtEOST, double *toccEOS,
+                    double *tvirtEOS, double *goccEOS, double *gvirtEOS);
+
+/* ---- energies (no counterpart in the reference: the reference stops at the
+ * amplitudes toccEOS/tvirtEOS and integrals goccEOS/gvirtEOS; the energy is
+ * the closed-shell MP2 expression built from the same g and denominator as
+ * RIMP2_calc_toccA, RIMP2.F90:397-404) --------------------------------------
+ * e_ij = sum_ab t_ij^ab (2 g_ij^ab - g_ij^ba),  t = g / (e_i+e_j-e_a-e_b),
+ * Epair(nocc,nocc) symmetric, Etot = sum_ij e_ij.
+ * precision: RIMP2_PREC_FP64 or RIMP2_PREC_SPLIT.  tamp (optional, may be
+ * NULL, FP64 path only) receives t(a,i,b,j) in layout (nvirt,nocc,nvirt,nocc). */
+int rimp2_energy(const int *nvirt, const int *nocc, const int *NBA, const double *Calpha,
+                 const double *EVocc, const double *EVvirt, double *Epair, double *Etot,
+                 double *tamp, const int *precision);
+
+/* Same with device pointers and by-value sizes, on `stream` (NULL = library
+ * stream).  Does not synchronise. */
+int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const double *dEVocc,
+                     const double *dEVvirt, double *dEpair, double *dEtot, double *dtamp,
+                     int precision, void *stream);
+
+/* Split form with an explicit slice count (1 = S0+R1, 2 = S0+R1+R2). */
+int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
+                           const double *dEVocc, const double *dEVvirt, double *dEpair,
+                           double *dEtot, int nslices, void *stream);
+
+/* Many DEC fragments of uneven size in one call.  Fragment f has sizes
+ * nocc[f], nvirt[f], NBA[f]; its Calpha/EVocc/EVvirt start at the given
+ * element offsets into the concatenated host arrays; Epair of fragment f
+ * starts at epair_off[f] (nocc[f]^2 entries), Etot[f] is its total. */
+int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, const int *NBA,
+                         const double *Calpha, const long long *calpha_off, const double *EVocc,
+                         const long long *eo_off, const double *EVvirt, const long long *ev_off,
+                         double *Epair, const long long *epair_off, double *Etot,
+                         const int *precision);
+
+/* ---- AO front end (no counterpart in the reference, whose input is already
+ * Calpha, RIMP2.F90:48-49) --------------------------------------------------
+ * Calpha(al,a,i) = sum_be Linv(al,be) sum_{mu,nu} Cmo(mu,nocc+a) Cmo(nu,i) ao(be,mu,nu)
+ * with V = L L^T the Cholesky factorisation of the auxiliary metric.  All
+ * FP64 on the GPU.  ao(NBA,nbas,nbas) symmetric in (mu,nu), V(NBA,NBA) SPD,
+ * Cmo(nbas,nbas) columns occ then virt; Calpha out (NBA,nvirt,nocc). */
+int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc, const int *nvirt,
+                         const double *ao, const double *V, const double *Cmo, double *Calpha);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RIMP2_GPU_H */

@@ -1,0 +1,209 @@
+"""Python mirror of the reference's subroutine interface, over the C-ABI.
+
+Every function keeps the argument list of the RIMP2.F90 subroutine it
+replaces (januseriksen/rimp2_gpu, file:line in each docstring); arrays are
+numpy ``float64`` in Fortran order with the reference's explicit shapes and
+outputs are written in place, as the Fortran ``intent(inout)`` dummies are.
+A failing call raises :class:`Rimp2Error` carrying the library's status and
+message; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import Rimp2Error, call, lib  # noqa: F401
+
+_dp = C.POINTER(C.c_double)
+
+PREC_FP64 = 0
+PREC_SPLIT = 1
+
+
+def _i(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _a(x, name, shape=None, writable=False):
+    if not isinstance(x, np.ndarray) or x.dtype != np.float64:
+        raise TypeError(f"{name} must be a float64 numpy array")
+    if not (x.flags.f_contiguous or x.ndim <= 1):
+        raise ValueError(f"{name} must be Fortran-ordered")
+    if shape is not None and x.size != int(np.prod(shape)):
+        raise ValueError(f"{name} has {x.size} elements, expected shape {tuple(shape)}")
+    if writable and not x.flags.writeable:
+        raise ValueError(f"{name} must be writable")
+    return x.ctypes.data_as(_dp)
+
+
+def calc_toccA(nvirt, nocc, noccEOS, NBA, Calpha, EVocc, EVvirt, tocc, UoccEOST):
+    """RIMP2_calc_toccA (RIMP2.F90:381-417)."""
+    call("rimp2_calc_tocca", _i(nvirt), _i(nocc), _i(noccEOS), _i(NBA),
+         _a(Calpha, "Calpha", (NBA, nvirt, nocc)), _a(EVocc, "EVocc", (nocc,)),
+         _a(EVvirt, "EVvirt", (nvirt,)), _a(tocc, "tocc", (nocc, noccEOS, nvirt, nvirt), True),
+         _a(UoccEOST, "UoccEOST", (nocc, noccEOS)))
+
+
+def calc_tvirtA(nvirt, nocc, nvirtEOS, NBA, Calpha, EVocc, EVvirt, tvirt, UvirtEOST):
+    """RIMP2_calc_tvirtA (RIMP2.F90:419-453)."""
+    call("rimp2_calc_tvirta", _i(nvirt), _i(nocc), _i(nvirtEOS), _i(NBA),
+         _a(Calpha, "Calpha", (NBA, nvirt, nocc)), _a(EVocc, "EVocc", (nocc,)),
+         _a(EVvirt, "EVvirt", (nvirt,)), _a(tvirt, "tvirt", (nocc, nocc, nvirtEOS, nvirt), True),
+         _a(UvirtEOST, "UvirtEOST", (nvirt, nvirtEOS)))
+
+
+def calc_toccB(nvirt, noccEOS, tocc, UvirtT, toccEOS):
+    """RIMP2_calc_toccB (RIMP2.F90:456-481)."""
+    call("rimp2_calc_toccb", _i(nvirt), _i(noccEOS),
+         _a(tocc, "tocc", (noccEOS, noccEOS, nvirt, nvirt)), _a(UvirtT, "UvirtT", (nvirt, nvirt)),
+         _a(toccEOS, "toccEOS", (nvirt, noccEOS, nvirt, noccEOS), True))
+
+
+def calc_tvirtB(nvirtEOS, nocc, tvirt, UoccT, tvirtEOS):
+    """RIMP2_calc_tvirtB (RIMP2.F90:483-508)."""
+    call("rimp2_calc_tvirtb", _i(nvirtEOS), _i(nocc),
+         _a(tvirt, "tvirt", (nocc, nocc, nvirtEOS, nvirtEOS)), _a(UoccT, "UoccT", (nocc, nocc)),
+         _a(tvirtEOS, "tvirtEOS", (nvirtEOS, nocc, nvirtEOS, nocc), True))
+
+
+def TransAlpha1(nvirt, noccEOS, nba, UvirtT, AlphaCD4, AlphaCD5):
+    """RIMP2_TransAlpha1 (RIMP2.F90:510-533)."""
+    call("rimp2_transalpha1", _i(nvirt), _i(noccEOS), _i(nba), _a(UvirtT, "UvirtT", (nvirt, nvirt)),
+         _a(AlphaCD4, "AlphaCD4", (nba, nvirt, noccEOS)),
+         _a(AlphaCD5, "AlphaCD5", (nba, nvirt, noccEOS), True))
+
+
+def TransAlpha2(n2, n1, n3, nba, U, AlphaCD4, AlphaCD5):
+    """RIMP2_TransAlpha2 (RIMP2.F90:536-560)."""
+    call("rimp2_transalpha2", _i(n2), _i(n1), _i(n3), _i(nba), _a(U, "U", (n1, n3)),
+         _a(AlphaCD4, "AlphaCD4", (nba, n1, n2)), _a(AlphaCD5, "AlphaCD5", (nba, n3, n2), True))
+
+
+def calc_gocc(nvirt, noccEOS, NBA, Calpha3, goccEOS):
+    """RIMP2_calc_gocc (RIMP2.F90:562-587)."""
+    call("rimp2_calc_gocc", _i(nvirt), _i(noccEOS), _i(NBA),
+         _a(Calpha3, "Calpha3", (NBA, nvirt, noccEOS)),
+         _a(goccEOS, "goccEOS", (nvirt, noccEOS, nvirt, noccEOS), True))
+
+
+def calc_gvirt(nvirtEOS, nocc, NBA, Calpha3, gvirtEOS):
+    """RIMP2_calc_gvirt (RIMP2.F90:589-614)."""
+    call("rimp2_calc_gvirt", _i(nvirtEOS), _i(nocc), _i(NBA),
+         _a(Calpha3, "Calpha3", (NBA, nvirtEOS, nocc)),
+         _a(gvirtEOS, "gvirtEOS", (nvirtEOS, nocc, nvirtEOS, nocc), True))
+
+
+def calc_gen4DimFO(NBA, Calpha3, n1, n2, Calpha4, n3, n4, djik):
+    """RIMP2_calc_gen4DimFO (RIMP2.F90:616-641)."""
+    call("rimp2_calc_gen4dimfo", _i(NBA), _a(Calpha3, "Calpha3", (NBA, n1, n2)), _i(n1), _i(n2),
+         _a(Calpha4, "Calpha4", (NBA, n3, n4)), _i(n3), _i(n4),
+         _a(djik, "djik", (n1, n2, n3, n4), True))
+
+
+def dgemm(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
+    """Column-major DGEMM as called at RIMP2.F90:79,87,110,118,137,160."""
+    call("rimp2_dgemm", transa.encode(), transb.encode(), _i(m), _i(n), _i(k),
+         C.byref(C.c_double(alpha)), _a(A, "A"), _i(lda), _a(B, "B"), _i(ldb),
+         C.byref(C.c_double(beta)), _a(Cm, "C", writable=True), _i(ldc))
+
+
+def steps5to8(nvirt, nocc, noccEOS, nvirtEOS, NBA, Calpha, EVocc, EVvirt, UoccEOST, UvirtT, UoccT,
+              UvirtEOST):
+    """Driver Steps 5-8 (RIMP2.F90:71-170) on the GPU; returns
+    (toccEOS, tvirtEOS, goccEOS, gvirtEOS)."""
+    f = lambda *s: np.zeros(s, dtype=np.float64, order="F")  # noqa: E731
+    toccEOS = f(nvirt, noccEOS, nvirt, noccEOS)
+    tvirtEOS = f(nvirtEOS, nocc, nvirtEOS, nocc)
+    goccEOS = f(nvirt, noccEOS, nvirt, noccEOS)
+    gvirtEOS = f(nvirtEOS, nocc, nvirtEOS, nocc)
+    call("rimp2_steps5to8", _i(nvirt), _i(nocc), _i(noccEOS), _i(nvirtEOS), _i(NBA),
+         _a(Calpha, "Calpha", (NBA, nvirt, nocc)), _a(EVocc, "EVocc"), _a(EVvirt, "EVvirt"),
+         _a(UoccEOST, "UoccEOST"), _a(UvirtT, "UvirtT"), _a(UoccT, "UoccT"),
+         _a(UvirtEOST, "UvirtEOST"), _a(toccEOS, "toccEOS", writable=True),
+         _a(tvirtEOS, "tvirtEOS", writable=True), _a(goccEOS, "goccEOS", writable=True),
+         _a(gvirtEOS, "gvirtEOS", writable=True))
+    return toccEOS, tvirtEOS, goccEOS, gvirtEOS
+
+
+def energy(nvirt, nocc, NBA, Calpha, EVocc, EVvirt, precision=PREC_FP64, amplitudes=False):
+    """MP2 pair energies and total from host arrays (C-ABI rimp2_energy).
+    Returns (Epair[nocc,nocc], Etot[, tamp(nvirt,nocc,nvirt,nocc)])."""
+    Ep = np.zeros((nocc, nocc), dtype=np.float64, order="F")
+    Et = np.zeros(1, dtype=np.float64)
+    t = np.zeros((nvirt, nocc, nvirt, nocc), dtype=np.float64, order="F") if amplitudes else None
+    call("rimp2_energy", _i(nvirt), _i(nocc), _i(NBA), _a(Calpha, "Calpha", (NBA, nvirt, nocc)),
+         _a(EVocc, "EVocc", (nocc,)), _a(EVvirt, "EVvirt", (nvirt,)), _a(Ep, "Epair", writable=True),
+         _a(Et, "Etot", writable=True), (_a(t, "tamp", writable=True) if t is not None else None),
+         _i(precision))
+    return (Ep, float(Et[0]), t) if amplitudes else (Ep, float(Et[0]))
+
+
+def energy_dev(nvirt, nocc, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot, dtamp=0,
+               precision=PREC_FP64, stream=0):
+    """Device-pointer form (integers are raw device addresses, e.g.
+    ``torch.Tensor.data_ptr()``); stream-ordered, no synchronisation."""
+    call("rimp2_energy_dev", nvirt, nocc, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot, dtamp or None,
+         precision, stream or None)
+
+
+def energy_split_dev(nvirt, nocc, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot, nslices=1,
+                     stream=0):
+    """Split-precision energy with an explicit residual-slice count."""
+    call("rimp2_energy_split_dev", nvirt, nocc, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot,
+         nslices, stream or None)
+
+
+def energy_batched(frags, precision=PREC_FP64):
+    """frags: list of (Calpha, EVocc, EVvirt) numpy arrays of uneven sizes.
+    Returns a list of (Epair, Etot)."""
+    nf = len(frags)
+    nocc = np.array([f[1].size for f in frags], dtype=np.int32)
+    nvirt = np.array([f[2].size for f in frags], dtype=np.int32)
+    nba = np.array([f[0].shape[0] for f in frags], dtype=np.int32)
+    ca = np.concatenate([np.asfortranarray(f[0]).ravel(order="F") for f in frags])
+    eo = np.concatenate([f[1] for f in frags])
+    ev = np.concatenate([f[2] for f in frags])
+    off = lambda sizes: np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)  # noqa: E731
+    ca_off = off([f[0].size for f in frags])
+    eo_off = off(nocc)
+    ev_off = off(nvirt)
+    ep_off = off(nocc.astype(np.int64) ** 2)
+    Ep = np.zeros(int((nocc.astype(np.int64) ** 2).sum()), dtype=np.float64)
+    Et = np.zeros(nf, dtype=np.float64)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
+    lp = lambda a: a.ctypes.data_as(C.POINTER(C.c_longlong))  # noqa: E731
+    call("rimp2_energy_batched", _i(nf), ip(nocc), ip(nvirt), ip(nba), _a(ca, "Calpha"), lp(ca_off),
+         _a(eo, "EVocc"), lp(eo_off), _a(ev, "EVvirt"), lp(ev_off), _a(Ep, "Epair", writable=True),
+         lp(ep_off), _a(Et, "Etot", writable=True), _i(precision))
+    out = []
+    for f in range(nf):
+        n = int(nocc[f])
+        out.append((Ep[ep_off[f]:ep_off[f] + n * n].reshape((n, n), order="F"), float(Et[f])))
+    return out
+
+
+def calpha_from_ao(NBA, nbas, nocc, nvirt, ao, V, Cmo):
+    """Calpha(NBA,nvirt,nocc) from AO three-centre integrals, metric and MO
+    coefficients (FP64 Cholesky + triangular solve on the GPU)."""
+    out = np.zeros((NBA, nvirt, nocc), dtype=np.float64, order="F")
+    call("rimp2_calpha_from_ao", _i(NBA), _i(nbas), _i(nocc), _i(nvirt),
+         _a(ao, "ao", (NBA, nbas, nbas)), _a(V, "V", (NBA, NBA)), _a(Cmo, "Cmo", (nbas, nbas)),
+         _a(out, "Calpha", writable=True))
+    return out
+
+
+def get_dev_mem():
+    """(total, free) device memory in bytes (replaces get_dev_mem, cuda_api.cu:5-8)."""
+    t = C.c_size_t()
+    f = C.c_size_t()
+    call("rimp2_get_dev_mem", C.byref(t), C.byref(f))
+    return t.value, f.value
+
+
+def kernel_launch_count():
+    return lib().rimp2_kernel_launch_count()
+
+
+def last_error():
+    return lib().rimp2_last_error_string().decode(errors="replace")

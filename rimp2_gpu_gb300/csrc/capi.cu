@@ -1,0 +1,720 @@
+// capi.cu -- thin C-ABI layer (the role cuda_api.cu plays in the reference):
+// argument validation, host<->device staging on the library stream, status
+// codes and error strings.  All arithmetic happens in the kernels of
+// fp64_kernels.cu, split_kernels.cu and front_end.cu; there is no host
+// compute path.
+#include <atomic>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace rimp2 {
+
+static thread_local char g_err[1024] = "";
+static std::atomic<long long> g_launches{0};
+static cudaStream_t g_user_stream = nullptr;
+static cudaStream_t g_lib_stream = nullptr;
+static std::mutex g_mu;
+static int g_dev_ok = -1;  // -1 unknown, 0 no, 1 yes
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+void clear_error() { g_err[0] = 0; }
+void count_launch(int n) { g_launches += n; }
+
+bool inject_fault(const char *what) {
+  const char *v = getenv("RIMP2_FAULT_INJECT");
+  return v && strcmp(v, what) == 0;
+}
+
+int DevBuf::alloc(size_t bytes, cudaStream_t st) {
+  s = st;
+  n = bytes;
+  if (bytes == 0) bytes = 16;
+  if (inject_fault("alloc")) {
+    set_error("injected device allocation failure (RIMP2_FAULT_INJECT=alloc)");
+    return RIMP2_ERR_NOMEM;
+  }
+  cudaError_t e = cudaMallocAsync(&p, bytes, st);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    return RIMP2_ERR_NOMEM;
+  }
+  return RIMP2_OK;
+}
+
+int ensure_device() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_dev_ok == 1) return RIMP2_OK;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    (void)cudaGetLastError();
+    set_error("no CUDA device available (%s); this library has no CPU path",
+              e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+    g_dev_ok = 0;
+    return RIMP2_ERR_NODEV;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    set_error("cudaGetDeviceProperties failed");
+    return RIMP2_ERR_NODEV;
+  }
+  if (!(prop.major == 10 && prop.minor == 3)) {
+    set_error("device %s is sm_%d%d; this library is built for sm_103a (GB300) only", prop.name,
+              prop.major, prop.minor);
+    g_dev_ok = 0;
+    return RIMP2_ERR_NODEV;
+  }
+  if (!g_lib_stream) {
+    if (cudaStreamCreateWithFlags(&g_lib_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      set_error("stream creation failed");
+      return RIMP2_ERR_CUDA;
+    }
+  }
+  g_dev_ok = 1;
+  return RIMP2_OK;
+}
+
+cudaStream_t current_stream() { return g_user_stream ? g_user_stream : g_lib_stream; }
+
+}  // namespace rimp2
+
+using namespace rimp2;
+
+namespace {
+
+int h2d(DevBuf &b, const double *h, size_t n, cudaStream_t s) {
+  RIMP2_TRY(b.alloc(n * sizeof(double), s));
+  RIMP2_CK(cudaMemcpyAsync(b.p, h, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  return RIMP2_OK;
+}
+int dalloc(DevBuf &b, size_t n, cudaStream_t s) { return b.alloc(n * sizeof(double), s); }
+int d2h(double *h, const DevBuf &b, size_t n, cudaStream_t s) {
+  RIMP2_CK(cudaMemcpyAsync(h, b.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  return RIMP2_OK;
+}
+int finish(cudaStream_t s) {
+  RIMP2_CK(cudaStreamSynchronize(s));
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+GemmDesc gd() {
+  GemmDesc g;
+  memset(&g, 0, sizeof g);
+  g.alpha = 1.0;
+  g.beta = 0.0;
+  g.nb0 = g.nb1 = 1;
+  return g;
+}
+
+// --- device-pointer building blocks ------------------------------------------
+
+// X(i,j,a,b) = g_ij(a,b) / D  (RIMP2.F90:397-404), X layout (nocc,nocc,nvirt,nvirt)
+int dev_g_over_d(int nvirt, int nocc, int NBA, const double *Ca, const double *eo,
+                 const double *ev, double *X, cudaStream_t s) {
+  GemmDesc g = gd();
+  const long long no = nocc, nv = nvirt, nb = NBA;
+  g.M = nvirt;
+  g.N = nvirt;
+  g.K = NBA;
+  g.A = Ca;
+  g.sAm = nb;
+  g.sAk = 1;
+  g.sAb0 = nb * nv;
+  g.B = Ca;
+  g.sBk = 1;
+  g.sBn = nb;
+  g.sBb1 = nb * nv;
+  g.C = X;
+  g.sCm = no * no;
+  g.sCn = no * no * nv;
+  g.sCb0 = 1;
+  g.sCb1 = no;
+  g.nb0 = nocc;
+  g.nb1 = nocc;
+  g.eo = eo;
+  g.ev = ev;
+  g.denom = 1;
+  return launch_gemm_f64(g, s);
+}
+
+int dev_tocca(int nvirt, int nocc, int noccEOS, int NBA, const double *Ca, const double *eo,
+              const double *ev, double *tocc, const double *U, cudaStream_t s) {
+  DevBuf X;
+  const size_t no = nocc, nv = nvirt;
+  RIMP2_TRY(dalloc(X, no * no * nv * nv, s));
+  RIMP2_TRY(dev_g_over_d(nvirt, nocc, NBA, Ca, eo, ev, X.as<double>(), s));
+  // tocc(i,jL,ab) = sum_j X(i,j,ab) U(j,jL)   (RIMP2.F90:406-412)
+  GemmDesc g = gd();
+  g.M = nvirt * nvirt;
+  g.N = noccEOS;
+  g.K = nocc;
+  g.A = X.as<double>();
+  g.sAm = (long long)no * no;
+  g.sAk = nocc;
+  g.sAb0 = 1;
+  g.B = U;
+  g.sBk = 1;
+  g.sBn = nocc;
+  g.C = tocc;
+  g.sCm = (long long)no * noccEOS;
+  g.sCn = nocc;
+  g.sCb0 = 1;
+  g.nb0 = nocc;
+  return launch_gemm_f64(g, s);
+}
+
+int dev_tvirta(int nvirt, int nocc, int nvirtEOS, int NBA, const double *Ca, const double *eo,
+               const double *ev, double *tvirt, const double *U, cudaStream_t s) {
+  DevBuf X;
+  const long long no = nocc, nv = nvirt;
+  RIMP2_TRY(dalloc(X, (size_t)(no * no * nv * nv), s));
+  RIMP2_TRY(dev_g_over_d(nvirt, nocc, NBA, Ca, eo, ev, X.as<double>(), s));
+  // tvirt(i,j,aL,b) = sum_a X(i,j,a,b) U(a,aL)   (RIMP2.F90:442-448)
+  GemmDesc g = gd();
+  g.M = nocc * nocc;
+  g.N = nvirtEOS;
+  g.K = nvirt;
+  g.A = X.as<double>();
+  g.sAm = 1;
+  g.sAk = no * no;
+  g.sAb0 = no * no * nv;
+  g.B = U;
+  g.sBk = 1;
+  g.sBn = nv;
+  g.C = tvirt;
+  g.sCm = 1;
+  g.sCn = no * no;
+  g.sCb0 = no * no * nvirtEOS;
+  g.nb0 = nvirt;
+  return launch_gemm_f64(g, s);
+}
+
+int dev_toccb(int nvirt, int noccEOS, const double *tocc, const double *UvirtT, double *toccEOS,
+              cudaStream_t s) {
+  GemmDesc g = gd();
+  const long long nv = nvirt, ne = noccEOS;
+  g.M = nvirt;
+  g.N = noccEOS;
+  g.K = nvirt;
+  g.A = UvirtT;
+  g.sAm = nv;
+  g.sAk = 1;
+  g.B = tocc;
+  g.sBk = ne * ne;
+  g.sBn = 1;
+  g.sBb0 = ne;
+  g.sBb1 = ne * ne * nv;
+  g.C = toccEOS;
+  g.sCm = 1;
+  g.sCn = nv;
+  g.sCb0 = nv * ne * nv;
+  g.sCb1 = nv * ne;
+  g.nb0 = noccEOS;
+  g.nb1 = nvirt;
+  return launch_gemm_f64(g, s);
+}
+
+int dev_tvirtb(int nvirtEOS, int nocc, const double *tvirt, const double *UoccT, double *tvirtEOS,
+               cudaStream_t s) {
+  GemmDesc g = gd();
+  const long long ve = nvirtEOS, no = nocc;
+  g.M = nocc;
+  g.N = nocc;
+  g.K = nocc;
+  g.A = tvirt;
+  g.sAm = 1;
+  g.sAk = no;
+  g.sAb0 = no * no;
+  g.sAb1 = no * no * ve;
+  g.B = UoccT;
+  g.sBk = 1;
+  g.sBn = no;
+  g.C = tvirtEOS;
+  g.sCm = ve;
+  g.sCn = ve * no * ve;
+  g.sCb0 = 1;
+  g.sCb1 = ve * no;
+  g.nb0 = nvirtEOS;
+  g.nb1 = nvirtEOS;
+  return launch_gemm_f64(g, s);
+}
+
+int dev_transalpha2(int n2, int n1, int n3, int nba, const double *U, const double *CD4,
+                    double *CD5, cudaStream_t s) {
+  GemmDesc g = gd();
+  const long long b = nba;
+  g.M = nba;
+  g.N = n3;
+  g.K = n1;
+  g.A = CD4;
+  g.sAm = 1;
+  g.sAk = b;
+  g.sAb0 = b * n1;
+  g.B = U;
+  g.sBk = 1;
+  g.sBn = n1;
+  g.C = CD5;
+  g.sCm = 1;
+  g.sCn = b;
+  g.sCb0 = b * n3;
+  g.nb0 = n2;
+  return launch_gemm_f64(g, s);
+}
+
+int dev_gen4dimfo(int NBA, const double *X, int n1, int n2, const double *Y, int n3, int n4,
+                  double *out, cudaStream_t s) {
+  GemmDesc g = gd();
+  const long long m = (long long)n1 * n2, n = (long long)n3 * n4;
+  if (m > 2147483647LL || n > 2147483647LL) {
+    set_error("gen4dimfo extents too large");
+    return RIMP2_ERR_ARG;
+  }
+  g.M = (int)m;
+  g.N = (int)n;
+  g.K = NBA;
+  g.A = X;
+  g.sAm = NBA;
+  g.sAk = 1;
+  g.B = Y;
+  g.sBk = 1;
+  g.sBn = NBA;
+  g.C = out;
+  g.sCm = 1;
+  g.sCn = m;
+  return launch_gemm_f64(g, s);
+}
+
+int dev_dgemm(char ta, char tb, int M, int N, int K, double alpha, const double *A, int lda,
+              const double *B, int ldb, double beta, double *Cm, int ldc, cudaStream_t s) {
+  GemmDesc g = gd();
+  const bool tA = (ta == 'T' || ta == 't' || ta == 'C' || ta == 'c');
+  const bool tB = (tb == 'T' || tb == 't' || tb == 'C' || tb == 'c');
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.alpha = alpha;
+  g.beta = beta;
+  g.A = A;
+  g.sAm = tA ? lda : 1;
+  g.sAk = tA ? 1 : lda;
+  g.B = B;
+  g.sBk = tB ? ldb : 1;
+  g.sBn = tB ? 1 : ldb;
+  g.C = Cm;
+  g.sCm = 1;
+  g.sCn = ldc;
+  return launch_gemm_f64(g, s);
+}
+
+bool pos(const int *p) { return p && *p > 0; }
+
+}  // namespace
+
+extern "C" {
+
+const char *rimp2_last_error_string(void) { return g_err; }
+const char *rimp2_version(void) { return "rimp2_gpu_gb300 0.1 (sm_103a)"; }
+long long rimp2_kernel_launch_count(void) { return g_launches.load(); }
+
+int rimp2_set_stream(void *stream) {
+  g_user_stream = (cudaStream_t)stream;
+  return RIMP2_OK;
+}
+
+int rimp2_get_dev_mem(size_t *total, size_t *free_bytes) {
+  clear_error();
+  RIMP2_REQ(total && free_bytes, "rimp2_get_dev_mem: null argument");
+  RIMP2_TRY(ensure_device());
+  RIMP2_CK(cudaMemGetInfo(free_bytes, total));
+  return RIMP2_OK;
+}
+
+int rimp2_calc_tocca(const int *nvirt, const int *nocc, const int *noccEOS, const int *NBA,
+                     const double *Calpha, const double *EVocc, const double *EVvirt, double *tocc,
+                     const double *UoccEOST) {
+  clear_error();
+  RIMP2_REQ(pos(nvirt) && pos(nocc) && pos(noccEOS) && pos(NBA), "rimp2_calc_tocca: bad dims");
+  RIMP2_REQ(Calpha && EVocc && EVvirt && tocc && UoccEOST, "rimp2_calc_tocca: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t nv = *nvirt, no = *nocc, ne = *noccEOS, nb = *NBA;
+  DevBuf dC, deo, dev, dU, dT;
+  RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
+  RIMP2_TRY(h2d(deo, EVocc, no, s));
+  RIMP2_TRY(h2d(dev, EVvirt, nv, s));
+  RIMP2_TRY(h2d(dU, UoccEOST, no * ne, s));
+  RIMP2_TRY(dalloc(dT, no * ne * nv * nv, s));
+  RIMP2_TRY(dev_tocca(*nvirt, *nocc, *noccEOS, *NBA, dC.as<double>(), deo.as<double>(),
+                      dev.as<double>(), dT.as<double>(), dU.as<double>(), s));
+  RIMP2_TRY(d2h(tocc, dT, no * ne * nv * nv, s));
+  return finish(s);
+}
+
+int rimp2_calc_tvirta(const int *nvirt, const int *nocc, const int *nvirtEOS, const int *NBA,
+                      const double *Calpha, const double *EVocc, const double *EVvirt,
+                      double *tvirt, const double *UvirtEOST) {
+  clear_error();
+  RIMP2_REQ(pos(nvirt) && pos(nocc) && pos(nvirtEOS) && pos(NBA), "rimp2_calc_tvirta: bad dims");
+  RIMP2_REQ(Calpha && EVocc && EVvirt && tvirt && UvirtEOST, "rimp2_calc_tvirta: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t nv = *nvirt, no = *nocc, ve = *nvirtEOS, nb = *NBA;
+  DevBuf dC, deo, dev, dU, dT;
+  RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
+  RIMP2_TRY(h2d(deo, EVocc, no, s));
+  RIMP2_TRY(h2d(dev, EVvirt, nv, s));
+  RIMP2_TRY(h2d(dU, UvirtEOST, nv * ve, s));
+  RIMP2_TRY(dalloc(dT, no * no * ve * nv, s));
+  RIMP2_TRY(dev_tvirta(*nvirt, *nocc, *nvirtEOS, *NBA, dC.as<double>(), deo.as<double>(),
+                       dev.as<double>(), dT.as<double>(), dU.as<double>(), s));
+  RIMP2_TRY(d2h(tvirt, dT, no * no * ve * nv, s));
+  return finish(s);
+}
+
+int rimp2_calc_toccb(const int *nvirt, const int *noccEOS, const double *tocc,
+                     const double *UvirtT, double *toccEOS) {
+  clear_error();
+  RIMP2_REQ(pos(nvirt) && pos(noccEOS), "rimp2_calc_toccb: bad dims");
+  RIMP2_REQ(tocc && UvirtT && toccEOS, "rimp2_calc_toccb: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t nv = *nvirt, ne = *noccEOS;
+  DevBuf dT, dU, dO;
+  RIMP2_TRY(h2d(dT, tocc, ne * ne * nv * nv, s));
+  RIMP2_TRY(h2d(dU, UvirtT, nv * nv, s));
+  RIMP2_TRY(dalloc(dO, nv * ne * nv * ne, s));
+  RIMP2_TRY(dev_toccb(*nvirt, *noccEOS, dT.as<double>(), dU.as<double>(), dO.as<double>(), s));
+  RIMP2_TRY(d2h(toccEOS, dO, nv * ne * nv * ne, s));
+  return finish(s);
+}
+
+int rimp2_calc_tvirtb(const int *nvirtEOS, const int *nocc, const double *tvirt,
+                      const double *UoccT, double *tvirtEOS) {
+  clear_error();
+  RIMP2_REQ(pos(nvirtEOS) && pos(nocc), "rimp2_calc_tvirtb: bad dims");
+  RIMP2_REQ(tvirt && UoccT && tvirtEOS, "rimp2_calc_tvirtb: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t ve = *nvirtEOS, no = *nocc;
+  DevBuf dT, dU, dO;
+  RIMP2_TRY(h2d(dT, tvirt, no * no * ve * ve, s));
+  RIMP2_TRY(h2d(dU, UoccT, no * no, s));
+  RIMP2_TRY(dalloc(dO, ve * no * ve * no, s));
+  RIMP2_TRY(dev_tvirtb(*nvirtEOS, *nocc, dT.as<double>(), dU.as<double>(), dO.as<double>(), s));
+  RIMP2_TRY(d2h(tvirtEOS, dO, ve * no * ve * no, s));
+  return finish(s);
+}
+
+int rimp2_transalpha2(const int *n2, const int *n1, const int *n3, const int *nba, const double *U,
+                      const double *AlphaCD4, double *AlphaCD5) {
+  clear_error();
+  RIMP2_REQ(pos(n2) && pos(n1) && pos(n3) && pos(nba), "rimp2_transalpha2: bad dims");
+  RIMP2_REQ(U && AlphaCD4 && AlphaCD5, "rimp2_transalpha2: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t a = *n2, b = *n1, c = *n3, nb = *nba;
+  DevBuf dU, d4, d5;
+  RIMP2_TRY(h2d(dU, U, b * c, s));
+  RIMP2_TRY(h2d(d4, AlphaCD4, nb * b * a, s));
+  RIMP2_TRY(dalloc(d5, nb * c * a, s));
+  RIMP2_TRY(dev_transalpha2(*n2, *n1, *n3, *nba, dU.as<double>(), d4.as<double>(), d5.as<double>(),
+                            s));
+  RIMP2_TRY(d2h(AlphaCD5, d5, nb * c * a, s));
+  return finish(s);
+}
+
+int rimp2_transalpha1(const int *nvirt, const int *noccEOS, const int *nba, const double *UvirtT,
+                      const double *AlphaCD4, double *AlphaCD5) {
+  // RIMP2_TransAlpha1 is RIMP2_TransAlpha2 with n2=noccEOS, n1=n3=nvirt
+  return rimp2_transalpha2(noccEOS, nvirt, nvirt, nba, UvirtT, AlphaCD4, AlphaCD5);
+}
+
+int rimp2_calc_gen4dimfo(const int *NBA, const double *Calpha3, const int *n1, const int *n2,
+                         const double *Calpha4, const int *n3, const int *n4, double *djik) {
+  clear_error();
+  RIMP2_REQ(pos(NBA) && pos(n1) && pos(n2) && pos(n3) && pos(n4), "rimp2_calc_gen4dimfo: bad dims");
+  RIMP2_REQ(Calpha3 && Calpha4 && djik, "rimp2_calc_gen4dimfo: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t nb = *NBA, a = *n1, b = *n2, c = *n3, d = *n4;
+  DevBuf dX, dY, dO;
+  RIMP2_TRY(h2d(dX, Calpha3, nb * a * b, s));
+  const double *yp = dX.as<double>();
+  if (Calpha4 != Calpha3) {
+    RIMP2_TRY(h2d(dY, Calpha4, nb * c * d, s));
+    yp = dY.as<double>();
+  }
+  RIMP2_TRY(dalloc(dO, a * b * c * d, s));
+  RIMP2_TRY(dev_gen4dimfo(*NBA, dX.as<double>(), *n1, *n2, yp, *n3, *n4, dO.as<double>(), s));
+  RIMP2_TRY(d2h(djik, dO, a * b * c * d, s));
+  return finish(s);
+}
+
+int rimp2_calc_gocc(const int *nvirt, const int *noccEOS, const int *NBA, const double *Calpha3,
+                    double *goccEOS) {
+  return rimp2_calc_gen4dimfo(NBA, Calpha3, nvirt, noccEOS, Calpha3, nvirt, noccEOS, goccEOS);
+}
+
+int rimp2_calc_gvirt(const int *nvirtEOS, const int *nocc, const int *NBA, const double *Calpha3,
+                     double *gvirtEOS) {
+  return rimp2_calc_gen4dimfo(NBA, Calpha3, nvirtEOS, nocc, Calpha3, nvirtEOS, nocc, gvirtEOS);
+}
+
+int rimp2_dgemm(const char *transa, const char *transb, const int *m, const int *n, const int *k,
+                const double *alpha, const double *A, const int *lda, const double *B,
+                const int *ldb, const double *beta, double *Cm, const int *ldc) {
+  clear_error();
+  RIMP2_REQ(transa && transb && m && n && k && alpha && beta && lda && ldb && ldc,
+            "rimp2_dgemm: null argument");
+  RIMP2_REQ(*m >= 0 && *n >= 0 && *k >= 0, "rimp2_dgemm: negative dims");
+  const char ta = *transa, tb = *transb;
+  RIMP2_REQ(strchr("NnTtCc", ta) && strchr("NnTtCc", tb), "rimp2_dgemm: bad trans flag");
+  const bool tA = !(ta == 'N' || ta == 'n'), tB = !(tb == 'N' || tb == 'n');
+  RIMP2_REQ(*lda >= (tA ? (*k > 1 ? *k : 1) : (*m > 1 ? *m : 1)), "rimp2_dgemm: lda too small");
+  RIMP2_REQ(*ldb >= (tB ? (*n > 1 ? *n : 1) : (*k > 1 ? *k : 1)), "rimp2_dgemm: ldb too small");
+  RIMP2_REQ(*ldc >= (*m > 1 ? *m : 1), "rimp2_dgemm: ldc too small");
+  if (*m == 0 || *n == 0) return RIMP2_OK;
+  RIMP2_REQ(Cm && (*k == 0 || (A && B)), "rimp2_dgemm: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t na = (size_t)*lda * (tA ? *m : *k), nbb = (size_t)*ldb * (tB ? *k : *n);
+  const size_t nc = (size_t)*ldc * *n;
+  DevBuf dA, dB, dCc;
+  if (*k > 0) {
+    RIMP2_TRY(h2d(dA, A, na, s));
+    RIMP2_TRY(h2d(dB, B, nbb, s));
+  }
+  if (*beta != 0.0)
+    RIMP2_TRY(h2d(dCc, Cm, nc, s));
+  else {
+    RIMP2_TRY(dalloc(dCc, nc, s));
+    RIMP2_CK(cudaMemsetAsync(dCc.p, 0, nc * sizeof(double), s));
+  }
+  if (*k > 0) {
+    RIMP2_TRY(dev_dgemm(ta, tb, *m, *n, *k, *alpha, dA.as<double>(), *lda, dB.as<double>(), *ldb,
+                        *beta, dCc.as<double>(), *ldc, s));
+  } else {
+    // C = beta*C: a K=0 product, done by the same kernel with a zero sum
+    RIMP2_TRY(dev_dgemm(ta, tb, *m, *n, 0, *alpha, dCc.as<double>(), 1, dCc.as<double>(), 1, *beta,
+                        dCc.as<double>(), *ldc, s));
+  }
+  RIMP2_TRY(d2h(Cm, dCc, nc, s));
+  return finish(s);
+}
+
+int rimp2_steps5to8(const int *nvirt_, const int *nocc_, const int *noccEOS_, const int *nvirtEOS_,
+                    const int *NBA_, const double *Calpha, const double *EVocc,
+                    const double *EVvirt, const double *UoccEOST, const double *UvirtT,
+                    const double *UoccT, const double *UvirtEOST, double *toccEOS,
+                    double *tvirtEOS, double *goccEOS, double *gvirtEOS) {
+  clear_error();
+  RIMP2_REQ(pos(nvirt_) && pos(nocc_) && pos(noccEOS_) && pos(nvirtEOS_) && pos(NBA_),
+            "rimp2_steps5to8: bad dims");
+  RIMP2_REQ(Calpha && EVocc && EVvirt && UoccEOST && UvirtT && UoccT && UvirtEOST && toccEOS &&
+                tvirtEOS && goccEOS && gvirtEOS,
+            "rimp2_steps5to8: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const int nvirt = *nvirt_, nocc = *nocc_, noccEOS = *noccEOS_, nvirtEOS = *nvirtEOS_,
+            NBA = *NBA_;
+  const size_t nv = nvirt, no = nocc, ne = noccEOS, ve = nvirtEOS, nb = NBA;
+  DevBuf dC, deo, dev, dUoE, dUvT, dUoT, dUvE;
+  RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
+  RIMP2_TRY(h2d(deo, EVocc, no, s));
+  RIMP2_TRY(h2d(dev, EVvirt, nv, s));
+  RIMP2_TRY(h2d(dUoE, UoccEOST, no * ne, s));
+  RIMP2_TRY(h2d(dUvT, UvirtT, nv * nv, s));
+  RIMP2_TRY(h2d(dUoT, UoccT, no * no, s));
+  RIMP2_TRY(h2d(dUvE, UvirtEOST, nv * ve, s));
+  const double *Ca = dC.as<double>(), *eo = deo.as<double>(), *ev = dev.as<double>();
+  {  // Step 5 (RIMP2.F90:71-93)
+    DevBuf t1, t2, t3, out;
+    RIMP2_TRY(dalloc(t1, no * ne * nv * nv, s));
+    RIMP2_TRY(dev_tocca(nvirt, nocc, noccEOS, NBA, Ca, eo, ev, t1.as<double>(), dUoE.as<double>(), s));
+    RIMP2_TRY(dalloc(t2, ne * ne * nv * nv, s));
+    RIMP2_TRY(dev_dgemm('T', 'N', noccEOS, noccEOS * nvirt * nvirt, nocc, 1.0, dUoE.as<double>(),
+                        nocc, t1.as<double>(), nocc, 0.0, t2.as<double>(), noccEOS, s));
+    RIMP2_TRY(dalloc(t3, nv * nv * ne * ne, s));
+    RIMP2_TRY(dev_dgemm('N', 'N', noccEOS * noccEOS * nvirt, nvirt, nvirt, 1.0, t2.as<double>(),
+                        noccEOS * noccEOS * nvirt, dUvT.as<double>(), nvirt, 0.0, t3.as<double>(),
+                        noccEOS * noccEOS * nvirt, s));
+    RIMP2_TRY(dalloc(out, nv * ne * nv * ne, s));
+    RIMP2_TRY(dev_toccb(nvirt, noccEOS, t3.as<double>(), dUvT.as<double>(), out.as<double>(), s));
+    RIMP2_TRY(d2h(toccEOS, out, nv * ne * nv * ne, s));
+    RIMP2_CK(cudaStreamSynchronize(s));
+  }
+  {  // Step 6 (RIMP2.F90:99-124)
+    DevBuf t1, t2, t3, out;
+    RIMP2_TRY(dalloc(t1, no * no * ve * nv, s));
+    RIMP2_TRY(dev_tvirta(nvirt, nocc, nvirtEOS, NBA, Ca, eo, ev, t1.as<double>(), dUvE.as<double>(), s));
+    RIMP2_TRY(dalloc(t2, no * no * ve * ve, s));
+    RIMP2_TRY(dev_dgemm('N', 'N', nocc * nocc * nvirtEOS, nvirtEOS, nvirt, 1.0, t1.as<double>(),
+                        nocc * nocc * nvirtEOS, dUvE.as<double>(), nvirt, 0.0, t2.as<double>(),
+                        nocc * nocc * nvirtEOS, s));
+    RIMP2_TRY(dalloc(t3, no * no * ve * ve, s));
+    RIMP2_TRY(dev_dgemm('T', 'N', nocc, nocc * nvirtEOS * nvirtEOS, nocc, 1.0, dUoT.as<double>(), nocc,
+                        t2.as<double>(), nocc, 0.0, t3.as<double>(), nocc, s));
+    RIMP2_TRY(dalloc(out, ve * no * ve * no, s));
+    RIMP2_TRY(dev_tvirtb(nvirtEOS, nocc, t3.as<double>(), dUoT.as<double>(), out.as<double>(), s));
+    RIMP2_TRY(d2h(tvirtEOS, out, ve * no * ve * no, s));
+    RIMP2_CK(cudaStreamSynchronize(s));
+  }
+  {  // Step 7 (RIMP2.F90:133-147)
+    DevBuf c2, c3, out;
+    RIMP2_TRY(dalloc(c2, nb * nv * ne, s));
+    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nvirt, noccEOS, nocc, 1.0, Ca, NBA * nvirt,
+                        dUoE.as<double>(), nocc, 0.0, c2.as<double>(), NBA * nvirt, s));
+    RIMP2_TRY(dalloc(c3, nb * nv * ne, s));
+    RIMP2_TRY(dev_transalpha2(noccEOS, nvirt, nvirt, NBA, dUvT.as<double>(), c2.as<double>(),
+                              c3.as<double>(), s));
+    RIMP2_TRY(dalloc(out, nv * ne * nv * ne, s));
+    RIMP2_TRY(dev_gen4dimfo(NBA, c3.as<double>(), nvirt, noccEOS, c3.as<double>(), nvirt, noccEOS,
+                            out.as<double>(), s));
+    RIMP2_TRY(d2h(goccEOS, out, nv * ne * nv * ne, s));
+    RIMP2_CK(cudaStreamSynchronize(s));
+  }
+  {  // Step 8 (RIMP2.F90:155-170)
+    DevBuf c2, c3, out;
+    RIMP2_TRY(dalloc(c2, nb * nv * no, s));
+    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nvirt, nocc, nocc, 1.0, Ca, NBA * nvirt, dUoT.as<double>(),
+                        nocc, 0.0, c2.as<double>(), NBA * nvirt, s));
+    RIMP2_TRY(dalloc(c3, nb * ve * no, s));
+    RIMP2_TRY(dev_transalpha2(nocc, nvirt, nvirtEOS, NBA, dUvE.as<double>(), c2.as<double>(),
+                              c3.as<double>(), s));
+    RIMP2_TRY(dalloc(out, ve * no * ve * no, s));
+    RIMP2_TRY(dev_gen4dimfo(NBA, c3.as<double>(), nvirtEOS, nocc, c3.as<double>(), nvirtEOS, nocc,
+                            out.as<double>(), s));
+    RIMP2_TRY(d2h(gvirtEOS, out, ve * no * ve * no, s));
+  }
+  return finish(s);
+}
+
+int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const double *dEVocc,
+                     const double *dEVvirt, double *dEpair, double *dEtot, double *dtamp,
+                     int precision, void *stream) {
+  clear_error();
+  RIMP2_REQ(nvirt > 0 && nocc > 0 && NBA > 0, "rimp2_energy_dev: bad dims");
+  RIMP2_REQ(dCalpha && dEVocc && dEVvirt && dEpair && dEtot, "rimp2_energy_dev: null array");
+  RIMP2_REQ(precision == RIMP2_PREC_FP64 || precision == RIMP2_PREC_SPLIT,
+            "rimp2_energy_dev: precision must be 0 (FP64) or 1 (split)");
+  RIMP2_REQ(!(precision == RIMP2_PREC_SPLIT && dtamp),
+            "rimp2_energy_dev: amplitudes are returned by the FP64 path only");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  if (precision == RIMP2_PREC_SPLIT)
+    return rimp2_energy_split_dev(nvirt, nocc, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot, 1,
+                                  stream);
+  PlainEnergyArgs a;
+  a.Ca = dCalpha;
+  a.NBA = NBA;
+  a.nvirt = nvirt;
+  a.nocc = nocc;
+  a.eo = dEVocc;
+  a.ev = dEVvirt;
+  a.Epair = dEpair;
+  a.Etot = dEtot;
+  a.tamp = dtamp;
+  a.pairs = nullptr;
+  a.npairs = 0;
+  return plain_energy_f64(a, s);
+}
+
+int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
+                           const double *dEVocc, const double *dEVvirt, double *dEpair,
+                           double *dEtot, int nslices, void *stream) {
+  clear_error();
+  RIMP2_REQ(nvirt > 0 && nocc > 0 && NBA > 0, "rimp2_energy_split_dev: bad dims");
+  RIMP2_REQ(dCalpha && dEVocc && dEVvirt && dEpair && dEtot, "rimp2_energy_split_dev: null array");
+  RIMP2_REQ(nslices == 1 || nslices == 2, "rimp2_energy_split_dev: nslices must be 1 or 2");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  SplitEnergyArgs a;
+  a.Ca = dCalpha;
+  a.NBA = NBA;
+  a.nvirt = nvirt;
+  a.nocc = nocc;
+  a.eo = dEVocc;
+  a.ev = dEVvirt;
+  a.Epair = dEpair;
+  a.Etot = dEtot;
+  a.nslices = nslices;
+  return split_energy(a, s, nullptr);
+}
+
+int rimp2_energy(const int *nvirt, const int *nocc, const int *NBA, const double *Calpha,
+                 const double *EVocc, const double *EVvirt, double *Epair, double *Etot,
+                 double *tamp, const int *precision) {
+  clear_error();
+  RIMP2_REQ(pos(nvirt) && pos(nocc) && pos(NBA), "rimp2_energy: bad dims");
+  RIMP2_REQ(Calpha && EVocc && EVvirt && Epair && Etot && precision, "rimp2_energy: null array");
+  RIMP2_REQ(*precision == RIMP2_PREC_FP64 || *precision == RIMP2_PREC_SPLIT,
+            "rimp2_energy: precision must be 0 (FP64) or 1 (split)");
+  RIMP2_REQ(!(*precision == RIMP2_PREC_SPLIT && tamp),
+            "rimp2_energy: amplitudes are returned by the FP64 path only");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const size_t nv = *nvirt, no = *nocc, nb = *NBA;
+  DevBuf dC, deo, dev, dE, dT, dA;
+  RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
+  RIMP2_TRY(h2d(deo, EVocc, no, s));
+  RIMP2_TRY(h2d(dev, EVvirt, nv, s));
+  RIMP2_TRY(dalloc(dE, no * no, s));
+  RIMP2_TRY(dalloc(dT, 1, s));
+  if (tamp) RIMP2_TRY(dalloc(dA, nv * no * nv * no, s));
+  RIMP2_TRY(rimp2_energy_dev(*nvirt, *nocc, *NBA, dC.as<double>(), deo.as<double>(),
+                             dev.as<double>(), dE.as<double>(), dT.as<double>(),
+                             tamp ? dA.as<double>() : nullptr, *precision, s));
+  RIMP2_TRY(d2h(Epair, dE, no * no, s));
+  RIMP2_TRY(d2h(Etot, dT, 1, s));
+  if (tamp) RIMP2_TRY(d2h(tamp, dA, nv * no * nv * no, s));
+  return finish(s);
+}
+
+int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, const int *NBA,
+                         const double *Calpha, const long long *calpha_off, const double *EVocc,
+                         const long long *eo_off, const double *EVvirt, const long long *ev_off,
+                         double *Epair, const long long *epair_off, double *Etot,
+                         const int *precision) {
+  clear_error();
+  RIMP2_REQ(nfrag && *nfrag >= 0, "rimp2_energy_batched: bad nfrag");
+  RIMP2_REQ(nocc && nvirt && NBA && Calpha && calpha_off && EVocc && eo_off && EVvirt && ev_off &&
+                Epair && epair_off && Etot && precision,
+            "rimp2_energy_batched: null argument");
+  for (int f = 0; f < *nfrag; ++f)
+    RIMP2_REQ(nocc[f] > 0 && nvirt[f] > 0 && NBA[f] > 0, "rimp2_energy_batched: bad dims in %d", f);
+  for (int f = 0; f < *nfrag; ++f) {
+    int rc = rimp2_energy(&nvirt[f], &nocc[f], &NBA[f], Calpha + calpha_off[f], EVocc + eo_off[f],
+                          EVvirt + ev_off[f], Epair + epair_off[f], Etot + f, nullptr, precision);
+    if (rc != RIMP2_OK) return rc;
+  }
+  return RIMP2_OK;
+}
+
+int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc, const int *nvirt,
+                         const double *ao, const double *V, const double *Cmo, double *Calpha) {
+  clear_error();
+  (void)NBA;
+  (void)nbas;
+  (void)nocc;
+  (void)nvirt;
+  (void)ao;
+  (void)V;
+  (void)Cmo;
+  (void)Calpha;
+  set_error("rimp2_calpha_from_ao: not built yet");
+  return RIMP2_ERR_UNSUPPORTED;
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+// common.cuh -- shared definitions of the rimp2_gpu_gb300 CUDA library.
+//
+// One process, one GPU, one library-owned CUDA stream (or a stream the caller
+// hands over).  Every C-ABI entry point returns an int status and never
+// aborts; the message of the last failure on the calling thread is kept for
+// rimp2_last_error_string().
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdarg.h>
+
+#include "../../include/rimp2_gpu.h"
+
+namespace rimp2 {
+
+// ---- status / error handling ------------------------------------------------
+void set_error(const char *fmt, ...);
+void clear_error();
+cudaStream_t current_stream();
+int ensure_device();  // RIMP2_OK or an error status (message set)
+
+#define RIMP2_CK(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      ::rimp2::set_error("%s:%d %s -> %s", __FILE__, __LINE__, #call,               \
+                         cudaGetErrorString(e_));                                   \
+      return e_ == cudaErrorMemoryAllocation ? RIMP2_ERR_NOMEM : RIMP2_ERR_CUDA;    \
+    }                                                                               \
+  } while (0)
+
+#define RIMP2_REQ(cond, ...)                  \
+  do {                                        \
+    if (!(cond)) {                            \
+      ::rimp2::set_error(__VA_ARGS__);        \
+      return RIMP2_ERR_ARG;                   \
+    }                                         \
+  } while (0)
+
+#define RIMP2_TRY(expr)          \
+  do {                           \
+    int s_ = (expr);             \
+    if (s_ != RIMP2_OK) return s_; \
+  } while (0)
+
+// Stream-ordered device buffer (memory pool backed); freed on scope exit.
+struct DevBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = nullptr;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  int alloc(size_t bytes, cudaStream_t st);
+  template <class T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
+// Host fault injection for failure-path tests: RIMP2_FAULT_INJECT=alloc makes
+// the next device allocation report out-of-memory, =launch makes the next
+// kernel-launch check report a launch failure.  Nothing touches the GPU.
+bool inject_fault(const char *what);
+
+// ---- FP64 DMMA kernels (fp64_kernels.cu) -------------------------------------
+struct GemmDesc {
+  int M, N, K;
+  double alpha, beta;
+  const double *A;
+  long long sAm, sAk, sAb0, sAb1;  // element strides: row m, reduction k, batch dims
+  const double *B;
+  long long sBk, sBn, sBb0, sBb1;
+  double *C;
+  long long sCm, sCn, sCb0, sCb1;
+  int nb0, nb1;  // batch extents (nb0 fastest)
+  // optional epilogue: divide by (eo[i]+eo[j]-ev[n]-ev[m]) where (i,j) come
+  // from the two batch indices (used by the toccA/tvirtA g/D step)
+  const double *eo, *ev;
+  int denom;  // 0 none, 1 batch=(i,j) row=a col=b
+};
+int launch_gemm_f64(const GemmDesc &g, cudaStream_t s);
+
+struct PlainEnergyArgs {
+  const double *Ca;  // Calpha(NBA, nvirt, nocc)
+  int NBA, nvirt, nocc;
+  const double *eo, *ev;
+  double *Epair;     // nocc*nocc (device)
+  double *Etot;      // 1 (device)
+  double *tamp;      // optional (nvirt, nocc, nvirt, nocc) (device) or null
+  const int *pairs;  // optional (i<=j) pairs list, device, 2*npairs; null = all
+  int npairs;
+};
+int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s);
+
+// ---- split-precision tcgen05 path (split_kernels.cu) ---------------------------
+struct SplitEnergyArgs {
+  const double *Ca;
+  int NBA, nvirt, nocc;
+  const double *eo, *ev;
+  double *Epair, *Etot;
+  int nslices;  // residual slices per element (1 or 2)
+};
+int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel);
+bool split_supported();
+
+}  // namespace rimp2

@@ -1,0 +1,383 @@
+// fp64_kernels.cu -- FP64 kernels on the DMMA (mma.sync .f64) tensor path.
+//
+//  * gemm_f64_kernel: strided, batched column-major-agnostic FP64 contraction
+//    C(m,n) = alpha * sum_k A(m,k) B(k,n) + beta * C(m,n) with an optional
+//    orbital-energy denominator epilogue.  It carries every FP64 product of
+//    the drop-in subroutines (toccA/tvirtA g/D and projections, toccB/tvirtB,
+//    TransAlpha1/2, gocc/gvirt/gen4DimFO, the driver's DGEMMs).
+//  * plain_energy_kernel: the fused FP64 energy kernel.  One CTA owns the tile
+//    pair (A,B) of occupied pair (i<=j): T1 = G_ij[A,B] = C_iA^T C_jB and
+//    T2 = G_ji[A,B] = C_jA^T C_iB share the (a,b) layout, so the exchange
+//    integral g_ij(b,a) sits in the same thread as g_ij(a,b) and the
+//    four-index integrals never leave the chip.
+//
+// GB300 FP64 throughput is a small fraction of its low-precision tensor
+// rate, so these kernels are arithmetic-bound by construction: shared-memory
+// staging is simple, padding keeps fragment loads bank-conflict free, and
+// the CTA count is large enough to fill all 152 SMs several times.
+#include "common.cuh"
+
+namespace rimp2 {
+
+namespace {
+
+constexpr int TM = 64;   // CTA tile rows
+constexpr int TN = 64;   // CTA tile cols
+constexpr int TK = 16;   // K slab
+constexpr int KP = 20;   // padded slab row (doubles): conflict-free 8x4 fragment reads
+constexpr int NTHR = 256;
+
+// D(8x8) += A(8x4, row) * B(4x8, col), FP64 tensor op.
+// Fragments: a = A[lane>>2][lane&3], b = B[lane&3][lane>>2],
+// d0/d1 = D[lane>>2][2*(lane&3) + 0/1].
+__device__ __forceinline__ void dmma884(double &d0, double &d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+// ---------------------------------------------------------------------------
+// Generic strided batched GEMM
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NTHR) gemm_f64_kernel(GemmDesc g) {
+  __shared__ double As[TM][KP];
+  __shared__ double Bs[TN][KP];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
+  const int gid = lane >> 2, tig = lane & 3;
+  const bool a_kcontig = (g.sAk == 1);
+  const bool b_kcontig = (g.sBk == 1);
+  const long long nbat = (long long)g.nb0 * g.nb1;
+
+  for (long long bz = blockIdx.z; bz < nbat; bz += gridDim.z) {
+    const int b0 = (int)(bz % g.nb0), b1 = (int)(bz / g.nb0);
+    const double *Ab = g.A + b0 * g.sAb0 + b1 * g.sAb1;
+    const double *Bb = g.B + b0 * g.sBb0 + b1 * g.sBb1;
+    double *Cb = g.C + b0 * g.sCb0 + b1 * g.sCb1;
+    for (int by = blockIdx.y; by * TN < g.N; by += gridDim.y) {
+      const int m0 = blockIdx.x * TM, n0 = by * TN;
+      double acc[4][2][2];
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) acc[x][y][0] = acc[x][y][1] = 0.0;
+
+      for (int k0 = 0; k0 < g.K; k0 += TK) {
+        // stage A(m0:m0+64, k0:k0+16) and B(k0:k0+16, n0:n0+64)
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          int mm, kk;
+          if (a_kcontig) {
+            kk = tid & 15;
+            mm = (tid >> 4) + 16 * p;
+          } else {
+            mm = tid & 63;
+            kk = (tid >> 6) + 4 * p;
+          }
+          const int m = m0 + mm, k = k0 + kk;
+          As[mm][kk] = (m < g.M && k < g.K) ? Ab[m * g.sAm + k * g.sAk] : 0.0;
+          int nn, kb;
+          if (b_kcontig) {
+            kb = tid & 15;
+            nn = (tid >> 4) + 16 * p;
+          } else {
+            nn = tid & 63;
+            kb = (tid >> 6) + 4 * p;
+          }
+          const int n = n0 + nn, kq = k0 + kb;
+          Bs[nn][kb] = (n < g.N && kq < g.K) ? Bb[kq * g.sBk + n * g.sBn] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < TK; ks += 4) {
+          double af[4], bf[2];
+#pragma unroll
+          for (int x = 0; x < 4; ++x) af[x] = As[wm + 8 * x + gid][ks + tig];
+#pragma unroll
+          for (int y = 0; y < 2; ++y) bf[y] = Bs[wn + 8 * y + gid][ks + tig];
+#pragma unroll
+          for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) dmma884(acc[x][y][0], acc[x][y][1], af[x], bf[y]);
+        }
+        __syncthreads();
+      }
+      // epilogue
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int m = m0 + wm + 8 * x + gid;
+            const int n = n0 + wn + 8 * y + 2 * tig + h;
+            if (m < g.M && n < g.N) {
+              double v = acc[x][y][h];
+              if (g.denom == 1) {
+                // RIMP2.F90:403-404: deltaEPS = EVocc(I)+EVocc(J)-EVvirt(B)-EVvirt(A)
+                const double d = g.eo[b0] + g.eo[b1] - g.ev[n] - g.ev[m];
+                v = v / d;
+              }
+              double *cp = Cb + m * g.sCm + n * g.sCn;
+              v = g.alpha * v;
+              if (g.beta != 0.0) v += g.beta * *cp;
+              *cp = v;
+            }
+          }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused FP64 energy kernel
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void decode_tri(int q, int &A, int &B) {
+  // q = B*(B+1)/2 + A, 0 <= A <= B
+  int b = (int)((sqrt(8.0 * q + 1.0) - 1.0) * 0.5);
+  while ((b + 1) * (b + 2) / 2 <= q) ++b;
+  while (b * (b + 1) / 2 > q) --b;
+  B = b;
+  A = q - b * (b + 1) / 2;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// part[item] = contribution of tile pair (A,B) to e_ij of pair p
+__global__ void __launch_bounds__(NTHR) plain_energy_kernel(const double *__restrict__ Ca, int NBA,
+                                                            int nvirt, int nocc,
+                                                            const double *__restrict__ eo,
+                                                            const double *__restrict__ ev,
+                                                            const int *__restrict__ pairs,
+                                                            int ntile, double *__restrict__ part,
+                                                            double *__restrict__ tamp) {
+  __shared__ double P[4][TM][KP];  // C_iA, C_jB, C_jA, C_iB slabs
+  __shared__ double red[NTHR / 32];
+  const int ntp = ntile * (ntile + 1) / 2;
+  const long long item = blockIdx.x;
+  const int p = (int)(item / ntp), q = (int)(item % ntp);
+  int tA, tB;
+  decode_tri(q, tA, tB);
+  const int i = pairs[2 * p], j = pairs[2 * p + 1];
+  const bool same = (i == j);
+  const int a0 = tA * TM, b0 = tB * TN;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
+  const int gid = lane >> 2, tig = lane & 3;
+  const size_t colstride = (size_t)NBA;
+  const double *ci = Ca + (size_t)NBA * nvirt * i;
+  const double *cj = Ca + (size_t)NBA * nvirt * j;
+
+  double t1[4][2][2], t2[4][2][2];
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 2; ++y) t1[x][y][0] = t1[x][y][1] = t2[x][y][0] = t2[x][y][1] = 0.0;
+
+  for (int k0 = 0; k0 < NBA; k0 += TK) {
+    const int kk = tid & 15;
+    const int k = k0 + kk;
+#pragma unroll
+    for (int pp = 0; pp < 4; ++pp) {
+      const int cc = (tid >> 4) + 16 * pp;  // column within tile
+      const int a = a0 + cc, b = b0 + cc;
+      const bool ka = (k < NBA);
+      P[0][cc][kk] = (ka && a < nvirt) ? ci[a * colstride + k] : 0.0;
+      P[1][cc][kk] = (ka && b < nvirt) ? cj[b * colstride + k] : 0.0;
+      if (!same) {
+        P[2][cc][kk] = (ka && a < nvirt) ? cj[a * colstride + k] : 0.0;
+        P[3][cc][kk] = (ka && b < nvirt) ? ci[b * colstride + k] : 0.0;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < TK; ks += 4) {
+      double a1[4], b1[2];
+#pragma unroll
+      for (int x = 0; x < 4; ++x) a1[x] = P[0][wm + 8 * x + gid][ks + tig];
+#pragma unroll
+      for (int y = 0; y < 2; ++y) b1[y] = P[1][wn + 8 * y + gid][ks + tig];
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) dmma884(t1[x][y][0], t1[x][y][1], a1[x], b1[y]);
+      if (!same) {
+        double a2[4], b2[2];
+#pragma unroll
+        for (int x = 0; x < 4; ++x) a2[x] = P[2][wm + 8 * x + gid][ks + tig];
+#pragma unroll
+        for (int y = 0; y < 2; ++y) b2[y] = P[3][wn + 8 * y + gid][ks + tig];
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 2; ++y) dmma884(t2[x][y][0], t2[x][y][1], a2[x], b2[y]);
+      }
+    }
+    __syncthreads();
+  }
+
+  // epilogue: denominators, amplitudes, energy contribution
+  const double eij = eo[i] + eo[j];
+  const bool diag = (tA == tB);
+  double e = 0.0;
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 2; ++y)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int a = a0 + wm + 8 * x + gid;
+        const int b = b0 + wn + 8 * y + 2 * tig + h;
+        if (a < nvirt && b < nvirt) {
+          const double g1 = t1[x][y][h];
+          const double g2 = same ? g1 : t2[x][y][h];
+          const double d = eij - ev[b] - ev[a];  // RIMP2.F90:403 order
+          const double u1 = g1 / d, u2 = g2 / d;
+          e += u1 * (2.0 * g1 - g2);
+          if (!diag) e += u2 * (2.0 * g2 - g1);
+          if (tamp) {
+            // t(a,i,b,j) = g_ij(a,b)/D ; t(b,i,a,j) = g_ij(b,a)/D
+            // t(a,j,b,i) = g_ji(a,b)/D = g_ij(b,a)/D ; t(b,j,a,i) = g_ij(a,b)/D
+            const size_t nv = nvirt, no = nocc;
+            tamp[a + nv * (i + no * (b + nv * j))] = u1;
+            if (!diag) tamp[b + nv * (i + no * (a + nv * j))] = u2;
+            if (!same) {
+              tamp[a + nv * (j + no * (b + nv * i))] = u2;
+              if (!diag) tamp[b + nv * (j + no * (a + nv * i))] = u1;
+            }
+          }
+        }
+      }
+  e = warp_sum(e);
+  if (lane == 0) red[warp] = e;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NTHR / 32; ++w) s += red[w];
+    part[item] = s;
+  }
+}
+
+}  // namespace
+
+// Neumaier-compensated reduction of the per-item partials into Epair and Etot.
+__global__ void pair_reduce_kernel(const double *__restrict__ part, int nper, const int *pairs,
+                                   int npairs, int nocc, double *Epair) {
+  const int p = blockIdx.x;
+  if (p >= npairs) return;
+  __shared__ double ss[256], sc[256];
+  double s = 0.0, c = 0.0;
+  for (int r = threadIdx.x; r < nper; r += blockDim.x) {
+    const double x = part[(size_t)p * nper + r];
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  ss[threadIdx.x] = s;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double S = 0.0, Cc = 0.0;
+    for (int t = 0; t < blockDim.x; ++t) {
+      const double x = ss[t];
+      const double u = S + x;
+      Cc += (fabs(S) >= fabs(x)) ? (S - u) + x : (x - u) + S;
+      S = u;
+      Cc += sc[t];
+    }
+    const double e = S + Cc;
+    const int i = pairs[2 * p], j = pairs[2 * p + 1];
+    Epair[i + (size_t)nocc * j] = e;
+    Epair[j + (size_t)nocc * i] = e;
+  }
+}
+
+// Etot = sum_ij Epair(i,j), compensated, one thread (nocc^2 is small).
+__global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double S = 0.0, Cc = 0.0;
+  for (size_t n = 0; n < (size_t)nocc * nocc; ++n) {
+    const double x = Epair[n];
+    const double u = S + x;
+    Cc += (fabs(S) >= fabs(x)) ? (S - u) + x : (x - u) + S;
+    S = u;
+  }
+  *Etot = S + Cc;
+}
+
+__global__ void make_pairs_kernel(int nocc, int *pairs) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = nocc * (nocc + 1) / 2;
+  if (n >= np) return;
+  int j = (int)((sqrt(8.0 * n + 1.0) - 1.0) * 0.5);
+  while ((j + 1) * (j + 2) / 2 <= n) ++j;
+  while (j * (j + 1) / 2 > n) --j;
+  pairs[2 * n] = n - j * (j + 1) / 2;
+  pairs[2 * n + 1] = j;
+}
+
+void count_launch(int n);
+
+int launch_gemm_f64(const GemmDesc &g, cudaStream_t s) {
+  if (g.M <= 0 || g.N <= 0 || g.nb0 <= 0 || g.nb1 <= 0) return RIMP2_OK;
+  if (inject_fault("launch")) {
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  long long mt = (g.M + TM - 1) / TM, nt = (g.N + TN - 1) / TN;
+  long long nb = (long long)g.nb0 * g.nb1;
+  if (mt > 2147483647LL) {
+    set_error("gemm M too large");
+    return RIMP2_ERR_ARG;
+  }
+  dim3 grid((unsigned)mt, (unsigned)(nt < 65535 ? nt : 65535), (unsigned)(nb < 65535 ? nb : 65535));
+  if (g.K <= 0) {
+    // C = beta*C (alpha*0): still run the kernel (it handles K=0 as zero sum)
+  }
+  gemm_f64_kernel<<<grid, NTHR, 0, s>>>(g);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s) {
+  const int ntile = (a.nvirt + TM - 1) / TM;
+  const int ntp = ntile * (ntile + 1) / 2;
+  const int npairs = a.pairs ? a.npairs : a.nocc * (a.nocc + 1) / 2;
+  DevBuf pairs_buf, part;
+  const int *pairs = a.pairs;
+  if (!pairs) {
+    RIMP2_TRY(pairs_buf.alloc(sizeof(int) * 2 * (size_t)npairs, s));
+    make_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(a.nocc, pairs_buf.as<int>());
+    count_launch(1);
+    RIMP2_CK(cudaGetLastError());
+    pairs = pairs_buf.as<int>();
+  }
+  const long long nitems = (long long)npairs * ntp;
+  if (nitems > 2147483647LL) {
+    set_error("too many work items (%lld)", nitems);
+    return RIMP2_ERR_ARG;
+  }
+  RIMP2_TRY(part.alloc(sizeof(double) * (size_t)nitems, s));
+  if (inject_fault("launch")) {
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  RIMP2_CK(cudaMemsetAsync(a.Epair, 0, sizeof(double) * (size_t)a.nocc * a.nocc, s));
+  plain_energy_kernel<<<(unsigned)nitems, NTHR, 0, s>>>(a.Ca, a.NBA, a.nvirt, a.nocc, a.eo, a.ev,
+                                                        pairs, ntile, part.as<double>(), a.tamp);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  pair_reduce_kernel<<<npairs, 256, 0, s>>>(part.as<double>(), ntp, pairs, npairs, a.nocc, a.Epair);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  total_reduce_kernel<<<1, 32, 0, s>>>(a.Epair, a.nocc, a.Etot);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+}  // namespace rimp2
