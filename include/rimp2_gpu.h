@@ -138,6 +138,10 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
                      const double *dEVvirt, double *dEpair, double *dEtot, double *dtamp,
                      int precision, void *stream);
 
+/* Residual-slice count the split form uses for a fragment of this shape
+ * (the per-shape-bucket choice that holds the energy error within 1e-7). */
+int rimp2_split_nslices(int nvirt, int nocc, int NBA);
+
 /* Split form with an explicit slice count (1 = S0+R1, 2 = S0+R1+R2). */
 int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
                            const double *dEVocc, const double *dEVvirt, double *dEpair,

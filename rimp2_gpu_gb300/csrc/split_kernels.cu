@@ -1,9 +1,650 @@
-// split_kernels.cu -- placeholder until the tcgen05 split-precision kernel lands.
+// split_kernels.cu -- split-precision RI-MP2 energy on the tcgen05 tensor cores.
+//
+// Numerics (Ozaki-style integer slices carried in FP16):
+//   For every column c=(a,i) of Calpha(:,a,i) a power-of-two scale s_c is
+//   chosen so that |C*s_c| <= 255.5 and ||round(C*s_c)||_2 <= 2^12.  Then
+//     C*s_c = S0 + R1 (+ R2)
+//   with S0 = round(C*s_c) an integer in [-256,256] (exact in FP16) and R1, R2
+//   the FP16-rounded residuals.  The alpha contraction of two columns is
+//     g*s_a*s_b = sum S0a S0b  +  sum (S0a R1b + R1a S0b + R1a R1b [+ S0a R2b + R2a S0b])
+//   The first sum (accumulator L0) is a sum of integers whose every partial
+//   sum is bounded by ||S0a|| ||S0b|| <= 2^24 (Cauchy-Schwarz), so the FP32
+//   tensor-core accumulation is EXACT whatever its internal rounding mode.
+//   The correction terms (accumulator L1) are ~2^-8 of g and uncorrelated
+//   with it, so their FP32 rounding does not bias the energy.
+//   The epilogue forms g in FP32, the denominator from hi/lo float pairs of
+//   the FP64 orbital energies, and accumulates e_ij in FP32 per thread and
+//   FP64 across threads; pair and total energies are reduced in FP64 with
+//   compensation.
+//
+// Kernel layout (one persistent CTA per SM, 192 threads):
+//   warp 0      TMA producer: 128x64 FP16 tiles (128B swizzle) of the slices
+//   warp 1      TMEM owner + single-thread tcgen05.mma issuer
+//   warps 2..5  epilogue: tcgen05.ld of the four accumulators, energy terms
+//   Work item = (pair i<=j, tile pair A<=B): T1 = G_ij[A,B] = C_iA^T C_jB and
+//   T2 = G_ji[A,B] = C_jA^T C_iB, each with L0/L1 accumulators in TMEM
+//   (4 x 128 columns = all 512).  The exchange integral g_ij(b,a) = T2[a,b]
+//   therefore lives in the same TMEM lane/column as g_ij(a,b) = T1[a,b], and
+//   no four-index quantity is ever written to memory.
+// Every wait on an mbarrier is bounded by a clock budget; on expiry the
+// kernel records an error code, drains its own copies and MMAs, frees TMEM
+// and returns, and the host reports RIMP2_ERR_TIMEOUT.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "common.cuh"
+
 namespace rimp2 {
-bool split_supported() { return false; }
-int split_energy(const SplitEnergyArgs &, cudaStream_t, float *) {
-  set_error("split-precision path not built yet");
-  return RIMP2_ERR_UNSUPPORTED;
+
+void count_launch(int n);
+__global__ void pair_reduce_kernel(const double *__restrict__ part, int nper, const int *pairs,
+                                   int npairs, int nocc, double *Epair);
+__global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot);
+__global__ void make_pairs_kernel(int nocc, int *pairs);
+
+namespace {
+
+constexpr int TILE = 128;      // a/b tile edge (MMA M and N)
+constexpr int KSTEP = 64;      // K per stage (one 128-byte swizzle row of FP16)
+constexpr int PANEL_BYTES = TILE * KSTEP * 2;  // 16 KB
+constexpr int NTHREADS = 192;
+constexpr long long WAIT_BUDGET = 4000000000LL;  // ~2 s of SM clock per wait
+
+// --------------------------------------------------------------------------
+// small PTX helpers
+// --------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: returns false (and raises the CTA abort flag and the global
+// error word) if the phase does not complete within the clock budget or if
+// another role already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                          int *err, int code) {
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (*abort_flag) return false;
+    if (clock64() - t0 > WAIT_BUDGET) {
+      *abort_flag = 1;
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, uint32_t bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// K-major operand tile of 128 rows x 64 FP16 (128-byte rows), 128B swizzle,
+// 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);          // start address
+  d |= (uint64_t)(16 >> 4) << 16;                  // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset: 8-row group pitch
+  d |= (uint64_t)1 << 46;                          // descriptor version (tcgen05)
+  d |= (uint64_t)2 << 61;                          // swizzle: 128B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A=B=F16, D=F32, K-major A and B, M=128, N=128
+constexpr uint32_t IDESC = (1u << 4)            // D format F32
+                           | (0u << 7)          // A format F16
+                           | (0u << 10)         // B format F16
+                           | ((uint32_t)(TILE >> 3) << 17)   // N >> 3
+                           | ((uint32_t)(TILE >> 4) << 24);  // M >> 4
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void decode_tri(int q, int &A, int &B) {
+  int b = (int)((sqrtf(8.0f * q + 1.0f) - 1.0f) * 0.5f);
+  while ((b + 1) * (b + 2) / 2 <= q) ++b;
+  while (b * (b + 1) / 2 > q) --b;
+  B = b;
+  A = q - b * (b + 1) / 2;
+}
+
+// --------------------------------------------------------------------------
+// slicing kernel: Calpha (FP64) -> FP16 slices + per-column inverse scales
+// --------------------------------------------------------------------------
+// slices layout: [slice][col][Kpad] FP16, col = a + nvpad*i (padded columns
+// and padded K are zero); inv_scale[col] = 2^-e.
+__global__ void slice_kernel(const double *__restrict__ Ca, int NBA, int nvirt, int nocc,
+                             int nvpad, int Kpad, int nsl, __half *__restrict__ slices,
+                             float *__restrict__ inv_scale) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int ncol = nvpad * nocc;
+  if (warp >= ncol) return;
+  const int a = warp % nvpad, i = warp / nvpad;
+  const size_t plane = (size_t)ncol * Kpad;
+  __half *s0 = slices + (size_t)warp * Kpad;
+  if (a >= nvirt) {
+    for (int k = lane; k < Kpad; k += 32)
+      for (int s = 0; s < nsl; ++s) s0[s * plane + k] = __float2half_rn(0.0f);
+    if (lane == 0) inv_scale[warp] = 1.0f;
+    return;
+  }
+  const double *c = Ca + ((size_t)i * nvirt + a) * NBA;
+  double mx = 0.0, ss = 0.0;
+  for (int k = lane; k < NBA; k += 32) {
+    const double v = c[k];
+    mx = fmax(mx, fabs(v));
+    ss += v * v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  }
+  int e = 0;
+  if (mx > 0.0) {
+    const double lim = fmin(255.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / sqrt(ss));
+    e = (int)floor(log2(lim));
+    e = max(-100, min(100, e));
+  }
+  for (int attempt = 0; attempt < 64; ++attempt) {
+    const double sc = ldexp(1.0, e);
+    double n2 = 0.0;
+    for (int k = lane; k < Kpad; k += 32) {
+      __half h0 = __float2half_rn(0.0f), h1 = h0, h2 = h0;
+      if (k < NBA) {
+        const double x = c[k] * sc;
+        const double q = rint(x);
+        const double r = x - q;  // exact
+        h0 = __double2half(q);   // integer |q| <= 256: exact
+        h1 = __double2half(r);
+        h2 = __double2half(r - (double)__half2float(h1));
+        n2 += q * q;
+      }
+      s0[k] = h0;
+      if (nsl > 1) s0[plane + k] = h1;
+      if (nsl > 2) s0[2 * plane + k] = h2;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+    if (n2 <= 16777216.0) break;  // ||S0||^2 <= 2^24: L0 accumulation exact
+    --e;
+  }
+  if (lane == 0) inv_scale[warp] = ldexpf(1.0f, -e);
+}
+
+// orbital energies as hi/lo float pairs (padded virtuals get a large value so
+// their denominators stay finite; their g is exactly zero)
+__global__ void eps_split_kernel(const double *eo, int nocc, const double *ev, int nvirt, int nvpad,
+                                 float2 *eo2, float2 *ev2) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nocc) {
+    const float h = (float)eo[t];
+    eo2[t] = make_float2(h, (float)(eo[t] - (double)h));
+  }
+  if (t < nvpad) {
+    const double v = t < nvirt ? ev[t] : 1000.0;
+    const float h = (float)v;
+    ev2[t] = make_float2(h, (float)(v - (double)h));
+  }
+}
+
+// --------------------------------------------------------------------------
+// the persistent split-precision energy kernel
+// --------------------------------------------------------------------------
+struct SplitParams {
+  int nocc, nvpad, ntile, ntp, nks, nsl, npairs;
+  long long nitems;
+  const int *pairs;        // (i<=j) pair list
+  const float2 *eo2;       // [nocc]
+  const float2 *ev2;       // [nvpad]
+  const float *inv_scale;  // [nocc*nvpad]
+  double *part;            // [nitems]
+  int *err;                // error word
+};
+
+template <int NSL, int NSTAGE>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    split_energy_kernel(const __grid_constant__ CUtensorMap tmap, SplitParams P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // 1024-aligned operand stages
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int STAGE_BYTES = NSL * 2 * PANEL_BYTES;
+  uint8_t *stages = base;
+  uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
+  // bars: full[NSTAGE], empty[NSTAGE], tmem_full, tmem_empty, drain
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NSTAGE + 3);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  float *red = (float *)(tmem_slot + 4);  // [4] epilogue warp partials (as double pairs)
+  double *redd = (double *)(((uintptr_t)(red) + 7) & ~(uintptr_t)7);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t full0 = smem_u32(&bars[0]);
+  const uint32_t empty0 = smem_u32(&bars[NSTAGE]);
+  const uint32_t tfull = smem_u32(&bars[2 * NSTAGE]);
+  const uint32_t tempty = smem_u32(&bars[2 * NSTAGE + 1]);
+  const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 2]);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, 4);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmap) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const long long nitems = P.nitems;
+  const int ntp = P.ntp, nks = P.nks, nvpad = P.nvpad;
+
+  if (warp == 0) {
+    // ------------------------------ TMA producer ------------------------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int armed[NSTAGE];
+      for (int s = 0; s < NSTAGE; ++s) armed[s] = -1;
+      bool ok = true;
+      for (long long it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+        const int p = (int)(it / ntp), q = (int)(it % ntp);
+        int tA, tB;
+        decode_tri(q, tA, tB);
+        const int i = P.pairs[2 * p], j = P.pairs[2 * p + 1];
+        const int ntiles = (i == j) ? 1 : 2;
+        for (int t = 0; t < ntiles && ok; ++t) {
+          const int colA = (t == 0 ? i : j) * nvpad + tA * TILE;
+          const int colB = (t == 0 ? j : i) * nvpad + tB * TILE;
+          for (int ks = 0; ks < nks; ++ks) {
+            if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err, 1)) {
+              ok = false;
+              break;
+            }
+            const uint32_t fb = full0 + 8 * stage;
+            mbar_expect_tx(fb, STAGE_BYTES);
+            armed[stage] = (int)phase;
+            const uint32_t dst = smem_u32(stages + stage * STAGE_BYTES);
+#pragma unroll
+            for (int sl = 0; sl < NSL; ++sl) {
+              tma_load_3d(dst + (2 * sl) * PANEL_BYTES, &tmap, fb, ks * KSTEP, colA, sl);
+              tma_load_3d(dst + (2 * sl + 1) * PANEL_BYTES, &tmap, fb, ks * KSTEP, colB, sl);
+            }
+            if (++stage == NSTAGE) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+      }
+      if (!ok) {  // drain copies in flight before the CTA can exit
+        for (int s = 0; s < NSTAGE; ++s) {
+          if (armed[s] < 0) continue;
+          const long long t0 = clock64();
+          while (!mbar_test(full0 + 8 * s, (uint32_t)armed[s]) && clock64() - t0 < WAIT_BUDGET) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------ MMA issuer --------------------------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      long long nloc = 0;
+      for (long long it = blockIdx.x; it < nitems && ok; it += gridDim.x, ++nloc) {
+        const int p = (int)(it / ntp);
+        const int i = P.pairs[2 * p], j = P.pairs[2 * p + 1];
+        const int ntiles = (i == j) ? 1 : 2;
+        if (nloc > 0) {  // epilogue must have drained TMEM of the previous item
+          if (!mbar_wait(tempty, (uint32_t)((nloc - 1) & 1), abort_flag, P.err, 2)) {
+            ok = false;
+            break;
+          }
+        }
+        tc_fence_after();
+        for (int t = 0; t < ntiles && ok; ++t) {
+          const uint32_t dL0 = tmem + (uint32_t)(t * 2 * TILE);
+          const uint32_t dL1 = dL0 + TILE;
+          for (int ks = 0; ks < nks; ++ks) {
+            if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err, 3)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sb = smem_u32(stages + stage * STAGE_BYTES);
+#pragma unroll
+            for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
+              const uint32_t koff = k16 * 32;  // bytes inside the 128-byte swizzle row
+              const uint64_t a0 = smem_desc(sb + 0 * PANEL_BYTES + koff);
+              const uint64_t b0 = smem_desc(sb + 1 * PANEL_BYTES + koff);
+              const uint64_t a1 = smem_desc(sb + 2 * PANEL_BYTES + koff);
+              const uint64_t b1 = smem_desc(sb + 3 * PANEL_BYTES + koff);
+              const uint32_t acc = (ks > 0 || k16 > 0) ? 1u : 0u;
+              mma_f16(dL0, a0, b0, acc);  // exact integer part
+              mma_f16(dL1, a0, b1, acc);  // S0a R1b
+              mma_f16(dL1, a1, b0, 1u);   // R1a S0b
+              mma_f16(dL1, a1, b1, 1u);   // R1a R1b
+              if (NSL > 2) {
+                const uint64_t a2 = smem_desc(sb + 4 * PANEL_BYTES + koff);
+                const uint64_t b2 = smem_desc(sb + 5 * PANEL_BYTES + koff);
+                mma_f16(dL1, a0, b2, 1u);  // S0a R2b
+                mma_f16(dL1, a2, b0, 1u);  // R2a S0b
+              }
+            }
+            mma_commit(empty0 + 8 * stage);  // frees the stage when these MMAs finish
+            if (++stage == NSTAGE) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+        if (ok) mma_commit(tfull);  // accumulators of this item complete
+      }
+      // drain: all MMAs issued by this thread complete before TMEM is freed
+      mma_commit(drain);
+      const long long t0 = clock64();
+      while (!mbar_test(drain, 0) && clock64() - t0 < WAIT_BUDGET) {
+      }
+    }
+  } else {
+    // ------------------------------ epilogue ----------------------------------
+    const int ew = warp - 2;           // 0..3
+    const int quad = warp & 3;         // TMEM lane quadrant this warp may access
+    const int row = quad * 32 + lane;  // tile row = a offset
+    long long nloc = 0;
+    for (long long it = blockIdx.x; it < nitems; it += gridDim.x, ++nloc) {
+      const int p = (int)(it / ntp), q = (int)(it % ntp);
+      int tA, tB;
+      decode_tri(q, tA, tB);
+      const int i = P.pairs[2 * p], j = P.pairs[2 * p + 1];
+      const bool same = (i == j), diag = (tA == tB);
+      if (!mbar_wait(tfull, (uint32_t)(nloc & 1), abort_flag, P.err, 4)) break;
+      tc_fence_after();
+      const int a = tA * TILE + row;
+      const float2 ea = P.ev2[a];
+      const float2 ei = P.eo2[i], ej = P.eo2[j];
+      // e_i + e_j in hi/lo form (two-sum of the hi parts, lo parts added)
+      const float sh = ei.x + ej.x;
+      const float bv = sh - ei.x;
+      const float sl = (ei.x - (sh - bv)) + (ej.x - bv) + ei.y + ej.y;
+      // per-row part of the denominator, again as an exact two-sum
+      const float dh0 = sh - ea.x;
+      const float bw = dh0 - sh;
+      const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
+      const float sa1 = P.inv_scale[i * nvpad + a];  // scale of column (a,i)
+      const float sa2 = P.inv_scale[j * nvpad + a];  // scale of column (a,j)
+      const float *sbj = P.inv_scale + j * nvpad + tB * TILE;
+      const float *sbi = P.inv_scale + i * nvpad + tB * TILE;
+      const float2 *evb = P.ev2 + tB * TILE;
+      const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+      const uint32_t t1 = tmem + lane_off;
+      const uint32_t t2 = same ? t1 : t1 + 2 * TILE;
+      double eacc = 0.0;
+#pragma unroll 1
+      for (int c0 = 0; c0 < TILE; c0 += 16) {
+        float l01[16], l11[16], l02[16], l12[16];
+        tmem_ld16(t1 + c0, l01);
+        tmem_ld16(t1 + TILE + c0, l11);
+        tmem_ld16(t2 + c0, l02);
+        tmem_ld16(t2 + TILE + c0, l12);
+        tmem_wait_ld();
+        float ef = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const int b = c0 + k;
+          const float2 eb = evb[b];
+          const float g1 = (l01[k] + l11[k]) * (sa1 * sbj[b]);
+          const float g2 = (l02[k] + l12[k]) * (sa2 * sbi[b]);
+          // d = (dh0 + dl0) - (eb.x + eb.y) with the leading subtraction exact
+          const float dh = dh0 - eb.x;
+          const float bz = dh - dh0;
+          const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
+          const float r = __frcp_rn(d);
+          float num;
+          if (diag) {
+            num = g1 * fmaf(2.0f, g1, -g2);
+          } else {
+            num = 2.0f * fmaf(g1, g1 - g2, g2 * g2);
+          }
+          ef = fmaf(num, r, ef);
+        }
+        eacc += (double)ef;
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty);
+      // reduce the item's energy over the 128 epilogue threads
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
+      if (lane == 0) redd[ew] = eacc;
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (ew == 0 && lane == 0) P.part[it] = (redd[0] + redd[1]) + (redd[2] + redd[3]);
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+// --------------------------------------------------------------------------
+// host side
+// --------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+int smem_bytes(int nsl, int nstage) {
+  return nstage * nsl * 2 * PANEL_BYTES + 1024 /*align*/ + 256 /*barriers etc*/;
+}
+
+template <int NSL, int NSTAGE>
+int launch_split(const CUtensorMap &tm, const SplitParams &P, int grid, cudaStream_t s) {
+  auto kern = split_energy_kernel<NSL, NSTAGE>;
+  const int smem = smem_bytes(NSL, NSTAGE);
+  RIMP2_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  kern<<<grid, NTHREADS, smem, s>>>(tm, P);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+}  // namespace
+
+bool split_supported() { return get_encode() != nullptr; }
+
+int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
+  (void)ms_kernel;
+  auto encode = get_encode();
+  if (!encode) {
+    set_error("cuTensorMapEncodeTiled entry point unavailable");
+    return RIMP2_ERR_UNSUPPORTED;
+  }
+  const int nsl = 1 + a.nslices;  // S0 + residual slices
+  const int nvpad = (a.nvirt + TILE - 1) / TILE * TILE;
+  const int Kpad = (a.NBA + KSTEP - 1) / KSTEP * KSTEP;
+  const int ntile = nvpad / TILE;
+  const int ntp = ntile * (ntile + 1) / 2;
+  const int npairs = a.nocc * (a.nocc + 1) / 2;
+  const long long ncol = (long long)nvpad * a.nocc;
+  const long long nitems = (long long)npairs * ntp;
+  if (ncol > (1LL << 31) - 1 || Kpad > (1 << 20)) {
+    set_error("split path: problem too large (ncol=%lld, Kpad=%d)", ncol, Kpad);
+    return RIMP2_ERR_ARG;
+  }
+  DevBuf slices, inv, eo2, ev2, pairs, part, err;
+  RIMP2_TRY(slices.alloc(sizeof(__half) * (size_t)nsl * ncol * Kpad, s));
+  RIMP2_TRY(inv.alloc(sizeof(float) * (size_t)ncol, s));
+  RIMP2_TRY(eo2.alloc(sizeof(float2) * (size_t)a.nocc, s));
+  RIMP2_TRY(ev2.alloc(sizeof(float2) * (size_t)nvpad, s));
+  RIMP2_TRY(pairs.alloc(sizeof(int) * 2 * (size_t)npairs, s));
+  RIMP2_TRY(part.alloc(sizeof(double) * (size_t)nitems, s));
+  RIMP2_TRY(err.alloc(sizeof(int), s));
+  RIMP2_CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+
+  {
+    const long long thr = ncol * 32;
+    slice_kernel<<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(
+        a.Ca, a.NBA, a.nvirt, a.nocc, nvpad, Kpad, nsl, slices.as<__half>(), inv.as<float>());
+    const int n = (a.nocc > nvpad ? a.nocc : nvpad);
+    eps_split_kernel<<<(n + 255) / 256, 256, 0, s>>>(a.eo, a.nocc, a.ev, a.nvirt, nvpad,
+                                                     eo2.as<float2>(), ev2.as<float2>());
+    make_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(a.nocc, pairs.as<int>());
+    count_launch(3);
+    RIMP2_CK(cudaGetLastError());
+  }
+
+  CUtensorMap tm;
+  cuuint64_t dims[3] = {(cuuint64_t)Kpad, (cuuint64_t)ncol, (cuuint64_t)nsl};
+  cuuint64_t strides[2] = {(cuuint64_t)Kpad * 2, (cuuint64_t)Kpad * 2 * (cuuint64_t)ncol};
+  cuuint32_t box[3] = {KSTEP, TILE, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult cr = encode(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, slices.p, dims, strides, box, estr,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+    return RIMP2_ERR_CUDA;
+  }
+
+  int dev = 0, nsm = 0;
+  RIMP2_CK(cudaGetDevice(&dev));
+  RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  SplitParams P;
+  P.nocc = a.nocc;
+  P.nvpad = nvpad;
+  P.ntile = ntile;
+  P.ntp = ntp;
+  P.nks = Kpad / KSTEP;
+  P.nsl = nsl;
+  P.npairs = npairs;
+  P.nitems = nitems;
+  P.pairs = pairs.as<int>();
+  P.eo2 = eo2.as<float2>();
+  P.ev2 = ev2.as<float2>();
+  P.inv_scale = inv.as<float>();
+  P.part = part.as<double>();
+  P.err = err.as<int>();
+  const int grid = (int)(nitems < nsm ? nitems : nsm);
+  if (inject_fault("launch")) {
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  if (nsl == 2)
+    RIMP2_TRY((launch_split<2, 3>(tm, P, grid, s)));
+  else
+    RIMP2_TRY((launch_split<3, 2>(tm, P, grid, s)));
+
+  RIMP2_CK(cudaMemsetAsync(a.Epair, 0, sizeof(double) * (size_t)a.nocc * a.nocc, s));
+  pair_reduce_kernel<<<npairs, 256, 0, s>>>(part.as<double>(), ntp, pairs.as<int>(), npairs, a.nocc,
+                                            a.Epair);
+  total_reduce_kernel<<<1, 32, 0, s>>>(a.Epair, a.nocc, a.Etot);
+  count_launch(2);
+  RIMP2_CK(cudaGetLastError());
+  int herr = 0;
+  RIMP2_CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RIMP2_CK(cudaStreamSynchronize(s));
+  if (herr) {
+    set_error("split energy kernel: bounded wait expired (code %d)", herr);
+    return RIMP2_ERR_TIMEOUT;
+  }
+  return RIMP2_OK;
+}
+
 }  // namespace rimp2

@@ -1,0 +1,77 @@
+"""Split-precision (tcgen05, FP16 Ozaki slices) energies against FP64.
+
+Bar: every pair energy and the total within 1e-7 relative of the FP64
+values, with the slice count the library picks for the shape; with two
+residual slices the contraction error is negligible and what remains is the
+FP32 epilogue's rounding (bar 3e-8).  Errors are printed
+for the record.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(16, 96, 384), (8, 64, 256), (5, 130, 200), (3, 300, 77), (12, 256, 1024),
+          (2, 128, 64), (1, 1, 1)]
+
+
+@pytest.fixture(scope="module")
+def api():
+    from rimp2_gpu_gb300 import api as A
+    return A
+
+
+def dev_energy(api, Ca, eo, ev, nslices):
+    import torch
+    NBA, nvirt, nocc = Ca.shape
+    dC = torch.from_numpy(Ca.ravel(order="F")).cuda()
+    deo, dev = torch.from_numpy(eo).cuda(), torch.from_numpy(ev).cuda()
+    dE = torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda")
+    dT = torch.zeros(1, dtype=torch.float64, device="cuda")
+    api.energy_split_dev(nvirt, nocc, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(),
+                         dE.data_ptr(), dT.data_ptr(), nslices=nslices)
+    torch.cuda.synchronize()
+    return dE.cpu().numpy().reshape(nocc, nocc, order="F"), dT.item()
+
+
+@pytest.mark.parametrize("nocc,nvirt,NBA", SHAPES)
+def test_split_energy_within_1e7(api, nocc, nvirt, NBA):
+    Ca, eo, ev = O.gen_fragment(200 + nvirt, nocc, nvirt, NBA)
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+    Ep, E = api.energy(nvirt, nocc, NBA, Ca, eo, ev, precision=api.PREC_SPLIT)
+    rel = np.abs(Ep - Epr) / np.abs(Epr)
+    tot = abs(E - Er) / abs(Er)
+    ns = api.lib().rimp2_split_nslices(nvirt, nocc, NBA)
+    print(f"\nsplit nocc={nocc} nvirt={nvirt} NBA={NBA} nslices={ns}: pair max {rel.max():.2e} "
+          f"mean {rel.mean():.2e} total {tot:.2e}")
+    assert rel.max() <= 1e-7
+    assert tot <= 1e-7
+
+
+@pytest.mark.parametrize("nocc,nvirt,NBA", SHAPES[:4])
+def test_split_two_slices_tight(api, nocc, nvirt, NBA):
+    Ca, eo, ev = O.gen_fragment(300 + nvirt, nocc, nvirt, NBA)
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+    for ns in (1, 2):
+        Ep, E = dev_energy(api, Ca, eo, ev, ns)
+        rel = np.abs(Ep - Epr) / np.abs(Epr)
+        print(f"\nnslices={ns} nocc={nocc} nvirt={nvirt} NBA={NBA}: pair max {rel.max():.2e} "
+              f"total {abs(E - Er) / abs(Er):.2e}")
+        if ns == 2:  # contraction error negligible; FP32 epilogue rounding remains
+            assert rel.max() <= 3e-8
+
+
+def test_split_exact_integer_part(api):
+    """Columns that are exact small integers times a power of two are sliced
+    with zero residual, so the split energy must equal FP64 to rounding of
+    the FP32 epilogue only (no contraction error at all)."""
+    nocc, nvirt, NBA = 3, 40, 96
+    rng = np.random.default_rng(0)
+    Ca = np.asfortranarray(rng.integers(-40, 41, size=(NBA, nvirt, nocc)).astype(np.float64) / 1024)
+    eo = np.sort(rng.uniform(-1.5, -0.3, nocc))
+    ev = np.sort(rng.uniform(0.1, 3.0, nvirt))
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev)
+    Ep, E = dev_energy(api, Ca, eo, ev, 1)
+    assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 2e-7
