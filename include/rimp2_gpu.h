@@ -50,6 +50,18 @@ int rimp2_set_stream(void *stream);
 int rimp2_get_dev_mem(size_t *total, size_t *free_bytes);
 /* Number of kernels this library has launched (all entry points). */
 long long rimp2_kernel_launch_count(void);
+/* Synchronise `stream` (NULL = library stream) and report any device-side
+ * failure of earlier *_dev calls (a bounded wait that expired inside a
+ * kernel): RIMP2_ERR_TIMEOUT, else RIMP2_OK.  Host-pointer entry points do
+ * this themselves before returning. */
+int rimp2_sync_status(void *stream);
+/* Opt-in CUDA-event timing of the split path's phases; rimp2_last_timing
+ * fills ms4 = {slicing, energy kernel, reductions, 0} of the last call. */
+int rimp2_set_timing(int on);
+int rimp2_last_timing(float *ms4);
+/* Measured FP64 tensor-op (DMMA) throughput of this GPU in TFLOP/s, the
+ * denominator for the plain kernel's roofline fraction. */
+int rimp2_probe_fp64_peak(double *tflops);
 
 /* ---- drop-in subroutines of RIMP2.F90 -----------------------------------
  * Each replaces the subroutine cited beside it; argument names, order and
@@ -133,7 +145,7 @@ int rimp2_energy(const int *nvirt, const int *nocc, const int *NBA, const double
                  double *tamp, const int *precision);
 
 /* Same with device pointers and by-value sizes, on `stream` (NULL = library
- * stream).  Does not synchronise. */
+ * stream).  Stream-ordered; does not synchronise (see rimp2_sync_status). */
 int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const double *dEVocc,
                      const double *dEVvirt, double *dEpair, double *dEtot, double *dtamp,
                      int precision, void *stream);
@@ -156,6 +168,14 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
                          const long long *eo_off, const double *EVvirt, const long long *ev_off,
                          double *Epair, const long long *epair_off, double *Etot,
                          const int *precision);
+
+/* ---- synthetic fragments (benchmark / test inputs; no counterpart in the
+ * reference, whose fixtures are constants written by generate.F90) --------
+ * Seeded Philox4x32-10 + Box-Muller on the device:
+ * Calpha(al,a,i) = N(0,1)*0.03/sqrt(1+al/64), EVocc sorted U[-1.5,-0.3],
+ * EVvirt sorted U[0.1,3.0].  Any output pointer may be NULL to skip it. */
+int rimp2_gen_fragment_dev(unsigned long long seed, int nocc, int nvirt, int NBA, double *dCalpha,
+                           double *dEVocc, double *dEVvirt, void *stream);
 
 /* ---- AO front end (no counterpart in the reference, whose input is already
  * Calpha, RIMP2.F90:48-49) --------------------------------------------------

@@ -69,6 +69,7 @@ def lib():
                 "orc_normal": [u64, u32, u64],
                 "orc_gen_calpha": [u64, i, i, i, _dp],
                 "orc_gen_eps": [u64, i, i, _dp, _dp],
+                "orc_gen_calpha_slabs": [u64, i, i, _ip, i, _dp],
                 "orc_gen_matrix": [u64, u32, i, i, _dp],
                 "orc_gen_kat": [i, i, i, i, i] + [_dp] * 7,
                 "orc_write_datafile": [C.c_char_p] + [i] * 6 + [_dp] * 11,
@@ -216,6 +217,14 @@ def gen_calpha(seed, NBA, nvirt, nocc):
     a = fzeros(NBA, nvirt, nocc)
     lib().orc_gen_calpha(seed, NBA, nvirt, nocc, _p(a))
     return a
+
+
+def gen_calpha_slabs(seed, NBA, nvirt, occ):
+    """Calpha(:,:,occ) of a fragment, generated for a subset of occupied indices."""
+    occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32))
+    out = fzeros(NBA, nvirt, occ.size)
+    lib().orc_gen_calpha_slabs(seed, NBA, nvirt, occ.ctypes.data_as(_ip), occ.size, _p(out))
+    return out
 
 
 def gen_eps(seed, nocc, nvirt):

@@ -316,24 +316,33 @@ double orc_pair_energies(int nvirt, int nocc, int NBA, const double *Calpha, con
       }
   }
   double *ep = (double *)malloc(sizeof(double) * (size_t)np);
+  /* one task per (pair, b): the b-loop of RIMP2.F90:395 is the parallel one,
+   * as in the reference's COLLAPSE over (BDIAG,ADIAG) */
+  double *part = (double *)malloc(sizeof(double) * (size_t)np * nvirt);
 #pragma omp parallel for schedule(dynamic, 1)
-  for (int p = 0; p < np; ++p) {
+  for (long long task = 0; task < (long long)np * nvirt; ++task) {
+    int p = (int)(task / nvirt), b = (int)(task % nvirt);
     int i = pl[2 * p], j = pl[2 * p + 1];
     double s = 0.0, c = 0.0;
-    for (int b = 0; b < nvirt; ++b)
-      for (int a = 0; a < nvirt; ++a) {
-        const double *cai = Calpha + I3(0, a, i, NBA, nvirt);
-        const double *cbj = Calpha + I3(0, b, j, NBA, nvirt);
-        const double *cbi = Calpha + I3(0, b, i, NBA, nvirt);
-        const double *caj = Calpha + I3(0, a, j, NBA, nvirt);
-        double g = 0.0, gx = 0.0;
-        for (int al = 0; al < NBA; ++al) g = g + cai[al] * cbj[al];
-        for (int al = 0; al < NBA; ++al) gx = gx + cbi[al] * caj[al];
-        double d = EVocc[i] + EVocc[j] - EVvirt[b] - EVvirt[a];
-        neumaier_add(&s, &c, (g / d) * (2.0 * g - gx));
-      }
+    for (int a = 0; a < nvirt; ++a) {
+      const double *cai = Calpha + I3(0, a, i, NBA, nvirt);
+      const double *cbj = Calpha + I3(0, b, j, NBA, nvirt);
+      const double *cbi = Calpha + I3(0, b, i, NBA, nvirt);
+      const double *caj = Calpha + I3(0, a, j, NBA, nvirt);
+      double g = 0.0, gx = 0.0;
+      for (int al = 0; al < NBA; ++al) g = g + cai[al] * cbj[al];   /* RIMP2.F90:400-402 */
+      for (int al = 0; al < NBA; ++al) gx = gx + cbi[al] * caj[al];
+      double d = EVocc[i] + EVocc[j] - EVvirt[b] - EVvirt[a];       /* RIMP2.F90:403 */
+      neumaier_add(&s, &c, (g / d) * (2.0 * g - gx));
+    }
+    part[task] = s + c;
+  }
+  for (int p = 0; p < np; ++p) {
+    double s = 0.0, c = 0.0;
+    for (int b = 0; b < nvirt; ++b) neumaier_add(&s, &c, part[(size_t)p * nvirt + b]);
     ep[p] = s + c;
   }
+  free(part);
   double ts = 0.0, tc = 0.0;
   for (int p = 0; p < np; ++p) {
     int i = pl[2 * p], j = pl[2 * p + 1];
@@ -518,6 +527,21 @@ void orc_gen_calpha(uint64_t seed, int NBA, int nvirt, int nocc, double *Calpha)
       int al1 = (int)((n + 1) % (size_t)NBA);
       Calpha[n + 1] = r * sin(th) * 0.03 / sqrt(1.0 + al1 / 64.0);
     }
+  }
+}
+
+/* Calpha(:,:,occ[k]) of the full fragment (nocc occupied) for a subset of
+ * occupied indices, written as out(NBA,nvirt,nsel): the same numbers
+ * orc_gen_calpha would put there. */
+void orc_gen_calpha_slabs(uint64_t seed, int NBA, int nvirt, const int *occ, int nsel, double *out) {
+  size_t slab = (size_t)NBA * nvirt;
+#pragma omp parallel for schedule(static)
+  for (long long t = 0; t < (long long)nsel * (long long)slab; ++t) {
+    int k = (int)(t / (long long)slab);
+    size_t r = (size_t)(t % (long long)slab);
+    size_t n = (size_t)occ[k] * slab + r;
+    int al = (int)(n % (size_t)NBA);
+    out[t] = philox_normal(seed, 0u, n) * 0.03 / sqrt(1.0 + al / 64.0);
   }
 }
 

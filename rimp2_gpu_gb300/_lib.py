@@ -27,6 +27,10 @@ SIGNATURES = {
     "rimp2_set_stream": ([_vp], C.c_int),
     "rimp2_get_dev_mem": ([C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], C.c_int),
     "rimp2_kernel_launch_count": ([], C.c_longlong),
+    "rimp2_sync_status": ([_vp], C.c_int),
+    "rimp2_set_timing": ([C.c_int], C.c_int),
+    "rimp2_last_timing": ([C.POINTER(C.c_float)], C.c_int),
+    "rimp2_probe_fp64_peak": ([_dp], C.c_int),
     "rimp2_calc_tocca": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp], C.c_int),
     "rimp2_calc_tvirta": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp], C.c_int),
     "rimp2_calc_toccb": ([_ip, _ip, _dp, _dp, _dp], C.c_int),
@@ -47,6 +51,8 @@ SIGNATURES = {
     "rimp2_split_nslices": ([C.c_int, C.c_int, C.c_int], C.c_int),
     "rimp2_energy_batched": ([_ip, _ip, _ip, _ip, _dp, _llp, _dp, _llp, _dp, _llp, _dp, _llp, _dp,
                               _ip], C.c_int),
+    "rimp2_gen_fragment_dev": ([C.c_ulonglong, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp],
+                               C.c_int),
     "rimp2_calpha_from_ao": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp], C.c_int),
 }
 

@@ -183,6 +183,12 @@ def energy_batched(frags, precision=PREC_FP64):
     return out
 
 
+def gen_fragment_dev(seed, nocc, nvirt, NBA, dCalpha=0, dEVocc=0, dEVvirt=0, stream=0):
+    """Generate a seeded synthetic fragment directly in device memory."""
+    call("rimp2_gen_fragment_dev", seed, nocc, nvirt, NBA, dCalpha or None, dEVocc or None,
+         dEVvirt or None, stream or None)
+
+
 def calpha_from_ao(NBA, nbas, nocc, nvirt, ao, V, Cmo):
     """Calpha(NBA,nvirt,nocc) from AO three-centre integrals, metric and MO
     coefficients (FP64 Cholesky + triangular solve on the GPU)."""
@@ -199,6 +205,29 @@ def get_dev_mem():
     f = C.c_size_t()
     call("rimp2_get_dev_mem", C.byref(t), C.byref(f))
     return t.value, f.value
+
+
+def sync_status(stream=0):
+    """Synchronise and raise if an earlier device-pointer call failed on the GPU."""
+    call("rimp2_sync_status", stream or None)
+
+
+def set_timing(on=True):
+    call("rimp2_set_timing", 1 if on else 0)
+
+
+def last_timing():
+    """(slicing_ms, energy_kernel_ms, reduction_ms) of the last split call."""
+    a = (C.c_float * 4)()
+    call("rimp2_last_timing", a)
+    return tuple(a[:3])
+
+
+def probe_fp64_peak():
+    """Measured FP64 DMMA throughput (TFLOP/s) of the current GPU."""
+    v = C.c_double()
+    call("rimp2_probe_fp64_peak", C.byref(v))
+    return v.value
 
 
 def kernel_launch_count():

@@ -18,6 +18,27 @@ static cudaStream_t g_user_stream = nullptr;
 static cudaStream_t g_lib_stream = nullptr;
 static std::mutex g_mu;
 static int g_dev_ok = -1;  // -1 unknown, 0 no, 1 yes
+static int *g_dev_err = nullptr;
+static bool g_timing = false;
+static float g_times[4] = {0, 0, 0, 0};
+
+int *device_error_word() { return g_dev_err; }
+bool timing_enabled() { return g_timing; }
+void record_timing(int slot, float ms) {
+  if (slot >= 0 && slot < 4) g_times[slot] = ms;
+}
+
+int collect_device_error(cudaStream_t s) {
+  RIMP2_CK(cudaStreamSynchronize(s));
+  int h = 0;
+  RIMP2_CK(cudaMemcpy(&h, g_dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h != 0) {
+    RIMP2_CK(cudaMemset(g_dev_err, 0, sizeof(int)));
+    set_error("a device-side bounded wait expired (code %d); the kernel returned early", h);
+    return RIMP2_ERR_TIMEOUT;
+  }
+  return RIMP2_OK;
+}
 
 void set_error(const char *fmt, ...) {
   va_list ap;
@@ -81,6 +102,20 @@ int ensure_device() {
       return RIMP2_ERR_CUDA;
     }
   }
+  if (!g_dev_err) {
+    if (cudaMalloc(&g_dev_err, sizeof(int)) != cudaSuccess ||
+        cudaMemset(g_dev_err, 0, sizeof(int)) != cudaSuccess) {
+      set_error("error-word allocation failed");
+      return RIMP2_ERR_NOMEM;
+    }
+  }
+  // keep freed stream-ordered scratch in the pool between calls instead of
+  // returning it to the driver at every synchronisation
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
   g_dev_ok = 1;
   return RIMP2_OK;
 }
@@ -106,7 +141,7 @@ int d2h(double *h, const DevBuf &b, size_t n, cudaStream_t s) {
 int finish(cudaStream_t s) {
   RIMP2_CK(cudaStreamSynchronize(s));
   RIMP2_CK(cudaGetLastError());
-  return RIMP2_OK;
+  return collect_device_error(s);
 }
 
 GemmDesc gd() {
@@ -327,6 +362,32 @@ extern "C" {
 const char *rimp2_last_error_string(void) { return g_err; }
 const char *rimp2_version(void) { return "rimp2_gpu_gb300 0.1 (sm_103a)"; }
 long long rimp2_kernel_launch_count(void) { return g_launches.load(); }
+
+int rimp2_sync_status(void *stream) {
+  clear_error();
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  RIMP2_CK(cudaGetLastError());
+  return collect_device_error(s);
+}
+
+int rimp2_set_timing(int on) {
+  g_timing = (on != 0);
+  return RIMP2_OK;
+}
+
+int rimp2_last_timing(float *ms4) {
+  if (!ms4) return RIMP2_ERR_ARG;
+  for (int k = 0; k < 4; ++k) ms4[k] = g_times[k];
+  return RIMP2_OK;
+}
+
+int rimp2_probe_fp64_peak(double *tflops) {
+  clear_error();
+  RIMP2_REQ(tflops, "rimp2_probe_fp64_peak: null argument");
+  RIMP2_TRY(ensure_device());
+  return probe_fp64_peak(tflops, current_stream());
+}
 
 int rimp2_set_stream(void *stream) {
   g_user_stream = (cudaStream_t)stream;

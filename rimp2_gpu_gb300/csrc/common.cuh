@@ -19,6 +19,11 @@ void set_error(const char *fmt, ...);
 void clear_error();
 cudaStream_t current_stream();
 int ensure_device();  // RIMP2_OK or an error status (message set)
+int *device_error_word();  // persistent device int that kernels set on a failed bounded wait
+int collect_device_error(cudaStream_t s);  // sync s, read + clear the word, map to a status
+// optional per-phase event timing of the split path (ms of the last call)
+bool timing_enabled();
+void record_timing(int slot, float ms);
 
 #define RIMP2_CK(call)                                                              \
   do {                                                                              \
@@ -94,6 +99,7 @@ struct PlainEnergyArgs {
   int npairs;
 };
 int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s);
+int probe_fp64_peak(double *tflops, cudaStream_t s);
 
 // ---- split-precision tcgen05 path (split_kernels.cu) ---------------------------
 struct SplitEnergyArgs {

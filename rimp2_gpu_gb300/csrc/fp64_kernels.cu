@@ -321,6 +321,48 @@ __global__ void make_pairs_kernel(int nocc, int *pairs) {
 
 void count_launch(int n);
 
+// FP64 tensor-op throughput probe: independent m8n8k4 DMMA chains, used to
+// report the plain kernel against the measured FP64 peak of this GPU.
+__global__ void dmma_probe_kernel(double *out, int iters) {
+  double d[8][2];
+  const double a = threadIdx.x * 1e-3, b = 1.0000001;
+#pragma unroll
+  for (int x = 0; x < 8; ++x) d[x][0] = d[x][1] = 0.0;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int x = 0; x < 8; ++x) dmma884(d[x][0], d[x][1], a, b);
+  double r = 0.0;
+#pragma unroll
+  for (int x = 0; x < 8; ++x) r += d[x][0] + d[x][1];
+  if (r == 1234.5) out[0] = r;  // keeps the chains live
+}
+
+int probe_fp64_peak(double *tflops, cudaStream_t s) {
+  int dev = 0, nsm = 0;
+  RIMP2_CK(cudaGetDevice(&dev));
+  RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  DevBuf o;
+  RIMP2_TRY(o.alloc(64, s));
+  const int blocks = nsm * 4, thr = 256, iters = 512;
+  dmma_probe_kernel<<<blocks, thr, 0, s>>>(o.as<double>(), 8);
+  cudaEvent_t e0, e1;
+  RIMP2_CK(cudaEventCreate(&e0));
+  RIMP2_CK(cudaEventCreate(&e1));
+  RIMP2_CK(cudaEventRecord(e0, s));
+  dmma_probe_kernel<<<blocks, thr, 0, s>>>(o.as<double>(), iters);
+  RIMP2_CK(cudaEventRecord(e1, s));
+  count_launch(2);
+  RIMP2_CK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  RIMP2_CK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // 8 chains x iters x (8x8x4 MACs per warp) x 2 FLOP
+  const double flop = 2.0 * 256.0 * 8.0 * iters * ((double)blocks * thr / 32.0);
+  *tflops = flop / (ms * 1e-3) / 1e12;
+  return RIMP2_OK;
+}
+
 int launch_gemm_f64(const GemmDesc &g, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.nb0 <= 0 || g.nb1 <= 0) return RIMP2_OK;
   if (inject_fault("launch")) {

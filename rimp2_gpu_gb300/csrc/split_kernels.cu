@@ -568,16 +568,18 @@ int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
     set_error("split path: problem too large (ncol=%lld, Kpad=%d)", ncol, Kpad);
     return RIMP2_ERR_ARG;
   }
-  DevBuf slices, inv, eo2, ev2, pairs, part, err;
+  DevBuf slices, inv, eo2, ev2, pairs, part;
   RIMP2_TRY(slices.alloc(sizeof(__half) * (size_t)nsl * ncol * Kpad, s));
   RIMP2_TRY(inv.alloc(sizeof(float) * (size_t)ncol, s));
   RIMP2_TRY(eo2.alloc(sizeof(float2) * (size_t)a.nocc, s));
   RIMP2_TRY(ev2.alloc(sizeof(float2) * (size_t)nvpad, s));
   RIMP2_TRY(pairs.alloc(sizeof(int) * 2 * (size_t)npairs, s));
   RIMP2_TRY(part.alloc(sizeof(double) * (size_t)nitems, s));
-  RIMP2_TRY(err.alloc(sizeof(int), s));
-  RIMP2_CK(cudaMemsetAsync(err.p, 0, sizeof(int), s));
-
+  const bool timed = timing_enabled();
+  cudaEvent_t ev[4];
+  if (timed)
+    for (int k = 0; k < 4; ++k) RIMP2_CK(cudaEventCreate(&ev[k]));
+  if (timed) RIMP2_CK(cudaEventRecord(ev[0], s));
   {
     const long long thr = ncol * 32;
     slice_kernel<<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(
@@ -620,16 +622,18 @@ int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
   P.ev2 = ev2.as<float2>();
   P.inv_scale = inv.as<float>();
   P.part = part.as<double>();
-  P.err = err.as<int>();
+  P.err = device_error_word();
   const int grid = (int)(nitems < nsm ? nitems : nsm);
   if (inject_fault("launch")) {
     set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
     return RIMP2_ERR_CUDA;
   }
+  if (timed) RIMP2_CK(cudaEventRecord(ev[1], s));
   if (nsl == 2)
     RIMP2_TRY((launch_split<2, 3>(tm, P, grid, s)));
   else
     RIMP2_TRY((launch_split<3, 2>(tm, P, grid, s)));
+  if (timed) RIMP2_CK(cudaEventRecord(ev[2], s));
 
   RIMP2_CK(cudaMemsetAsync(a.Epair, 0, sizeof(double) * (size_t)a.nocc * a.nocc, s));
   pair_reduce_kernel<<<npairs, 256, 0, s>>>(part.as<double>(), ntp, pairs.as<int>(), npairs, a.nocc,
@@ -637,12 +641,15 @@ int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
   total_reduce_kernel<<<1, 32, 0, s>>>(a.Epair, a.nocc, a.Etot);
   count_launch(2);
   RIMP2_CK(cudaGetLastError());
-  int herr = 0;
-  RIMP2_CK(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  RIMP2_CK(cudaStreamSynchronize(s));
-  if (herr) {
-    set_error("split energy kernel: bounded wait expired (code %d)", herr);
-    return RIMP2_ERR_TIMEOUT;
+  if (timed) {
+    RIMP2_CK(cudaEventRecord(ev[3], s));
+    RIMP2_CK(cudaEventSynchronize(ev[3]));
+    float ms;
+    for (int k = 0; k < 3; ++k) {
+      RIMP2_CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+      record_timing(k, ms);
+    }
+    for (int k = 0; k < 4; ++k) cudaEventDestroy(ev[k]);
   }
   return RIMP2_OK;
 }

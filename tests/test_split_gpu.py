@@ -75,3 +75,17 @@ def test_split_exact_integer_part(api):
     Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev)
     Ep, E = dev_energy(api, Ca, eo, ev, 1)
     assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 2e-7
+
+
+def test_device_generator_matches_oracle(api):
+    import torch
+    nocc, nvirt, NBA = 5, 33, 70
+    Ca, eo, ev = O.gen_fragment(9, nocc, nvirt, NBA)
+    dC = torch.zeros(NBA * nvirt * nocc, dtype=torch.float64, device="cuda")
+    deo = torch.zeros(nocc, dtype=torch.float64, device="cuda")
+    dev = torch.zeros(nvirt, dtype=torch.float64, device="cuda")
+    api.gen_fragment_dev(9, nocc, nvirt, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr())
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(dC.cpu().numpy(), Ca.ravel(order="F"), rtol=1e-13, atol=1e-17)
+    np.testing.assert_allclose(deo.cpu().numpy(), eo, rtol=1e-15)
+    np.testing.assert_allclose(dev.cpu().numpy(), ev, rtol=1e-15)
