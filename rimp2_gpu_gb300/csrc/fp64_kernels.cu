@@ -263,49 +263,76 @@ __global__ void __launch_bounds__(NTHR) plain_energy_kernel(const double *__rest
 
 }  // namespace
 
-// Neumaier-compensated reduction of the per-item partials into Epair and Etot.
-__global__ void pair_reduce_kernel(const double *__restrict__ part, int nper, const int *pairs,
-                                   int npairs, int nocc, double *Epair) {
-  const int p = blockIdx.x;
-  if (p >= npairs) return;
-  __shared__ double ss[256], sc[256];
-  double s = 0.0, c = 0.0;
-  for (int r = threadIdx.x; r < nper; r += blockDim.x) {
-    const double x = part[(size_t)p * nper + r];
-    const double t = s + x;
-    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+// Compensated reductions (deterministic: fixed assignment and fixed tree).
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void warp_sum_comp(double &s, double &c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double s2 = __shfl_xor_sync(0xffffffffu, s, o);
+    const double c2 = __shfl_xor_sync(0xffffffffu, c, o);
+    double t, e;
+    // order the operands so every lane combines the same way
+    if ((threadIdx.x & o) == 0)
+      two_sum(s, s2, t, e);
+    else
+      two_sum(s2, s, t, e);
     s = t;
-  }
-  ss[threadIdx.x] = s;
-  sc[threadIdx.x] = c;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double S = 0.0, Cc = 0.0;
-    for (int t = 0; t < blockDim.x; ++t) {
-      const double x = ss[t];
-      const double u = S + x;
-      Cc += (fabs(S) >= fabs(x)) ? (S - u) + x : (x - u) + S;
-      S = u;
-      Cc += sc[t];
-    }
-    const double e = S + Cc;
-    const int i = pairs[2 * p], j = pairs[2 * p + 1];
-    Epair[i + (size_t)nocc * j] = e;
-    Epair[j + (size_t)nocc * i] = e;
+    c = ((threadIdx.x & o) == 0 ? c + c2 : c2 + c) + e;
   }
 }
 
-// Etot = sum_ij Epair(i,j), compensated, one thread (nocc^2 is small).
-__global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double S = 0.0, Cc = 0.0;
-  for (size_t n = 0; n < (size_t)nocc * nocc; ++n) {
-    const double x = Epair[n];
-    const double u = S + x;
-    Cc += (fabs(S) >= fabs(x)) ? (S - u) + x : (x - u) + S;
-    S = u;
+// one warp per pair: Epair(i,j) = Epair(j,i) = compensated sum of its items
+__global__ void pair_reduce_kernel(const double *__restrict__ part, int nper, const int *pairs,
+                                   int npairs, int nocc, double *Epair) {
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (p >= npairs) return;
+  double s = 0.0, c = 0.0;
+  for (int r = lane; r < nper; r += 32) {
+    double t, e;
+    two_sum(s, part[(size_t)p * nper + r], t, e);
+    s = t;
+    c += e;
   }
-  *Etot = S + Cc;
+  warp_sum_comp(s, c);
+  if (lane == 0) {
+    const double v = s + c;
+    const int i = pairs[2 * p], j = pairs[2 * p + 1];
+    Epair[i + (size_t)nocc * j] = v;
+    Epair[j + (size_t)nocc * i] = v;
+  }
+}
+
+// Etot = sum_ij Epair(i,j): one block of 1024 threads, compensated tree
+__global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot) {
+  __shared__ double ss[32], sc[32];
+  double s = 0.0, c = 0.0;
+  const size_t n = (size_t)nocc * nocc;
+  for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
+    double t, e;
+    two_sum(s, Epair[k], t, e);
+    s = t;
+    c += e;
+  }
+  warp_sum_comp(s, c);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    ss[w] = s;
+    sc[w] = c;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    s = lane < nw ? ss[lane] : 0.0;
+    c = lane < nw ? sc[lane] : 0.0;
+    warp_sum_comp(s, c);
+    if (lane == 0) *Etot = s + c;
+  }
 }
 
 __global__ void make_pairs_kernel(int nocc, int *pairs) {
@@ -413,10 +440,11 @@ int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s) {
                                                         pairs, ntile, part.as<double>(), a.tamp);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
-  pair_reduce_kernel<<<npairs, 256, 0, s>>>(part.as<double>(), ntp, pairs, npairs, a.nocc, a.Epair);
+  pair_reduce_kernel<<<(npairs + 7) / 8, 256, 0, s>>>(part.as<double>(), ntp, pairs, npairs, a.nocc,
+                                                     a.Epair);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
-  total_reduce_kernel<<<1, 32, 0, s>>>(a.Epair, a.nocc, a.Etot);
+  total_reduce_kernel<<<1, 1024, 0, s>>>(a.Epair, a.nocc, a.Etot);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;

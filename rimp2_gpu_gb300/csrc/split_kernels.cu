@@ -182,6 +182,39 @@ __device__ __forceinline__ void decode_tri(int q, int &A, int &B) {
 // --------------------------------------------------------------------------
 // slices layout: [slice][col][Kpad] FP16, col = a + nvpad*i (padded columns
 // and padded K are zero); inv_scale[col] = 2^-e.
+//
+// GB300 runs FP64 arithmetic at a small fraction of its FP32 rate, so the
+// per-element work here avoids the FP64 pipe: the double is split into an
+// exact float pair (xh, xl) by bit manipulation, with the power-of-two scale
+// applied to the exponent field, and rounding/residuals are taken in FP32
+// where they are exact or carry ~2^-48 relative error.  Only the per-column
+// scale choice uses FP64.
+__device__ __forceinline__ float bits_to_float_trunc(unsigned long long b, int add_exp) {
+  // double bits -> float with truncated mantissa, exponent shifted by add_exp;
+  // caller guarantees the result is a normal float or zero
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  if (mag == 0) return 0.0f;
+  const int ex = (int)(mag >> 52) - 1023 + add_exp;
+  if (ex < -126) return 0.0f;  // below float range: negligible against |C*s| <= 256
+  if (ex > 127) return __uint_as_float(((uint32_t)(b >> 63) << 31) | 0x7F800000u);
+  const uint32_t mant = (uint32_t)((mag >> 29) & 0x7FFFFFu);
+  const uint32_t sign = (uint32_t)(b >> 63) << 31;
+  return __uint_as_float(sign | ((uint32_t)(ex + 127) << 23) | mant);
+}
+
+__device__ __forceinline__ void split_double(double c, int e, float &xh, float &xl) {
+  // x = c * 2^e = xh + xl, xh = x truncated to 24 bits, xl = rest (rounded to 24 bits)
+  const unsigned long long b = (unsigned long long)__double_as_longlong(c);
+  xh = bits_to_float_trunc(b, e);
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  const int ex = (int)(mag >> 52) - 1023 + e;
+  const unsigned long long low = mag & 0x1FFFFFFFull;  // 29 mantissa bits below xh
+  float l = (float)(unsigned int)low;                  // exact to 24 bits
+  l = ldexpf(l, ex - 52);
+  xl = (b >> 63) ? -l : l;
+  if (mag == 0 || ex < -126) xl = 0.0f;
+}
+
 __global__ void slice_kernel(const double *__restrict__ Ca, int NBA, int nvirt, int nocc,
                              int nvpad, int Kpad, int nsl, __half *__restrict__ slices,
                              float *__restrict__ inv_scale) {
@@ -192,43 +225,54 @@ __global__ void slice_kernel(const double *__restrict__ Ca, int NBA, int nvirt, 
   const int a = warp % nvpad, i = warp / nvpad;
   const size_t plane = (size_t)ncol * Kpad;
   __half *s0 = slices + (size_t)warp * Kpad;
+  const __half hz = __float2half_rn(0.0f);
   if (a >= nvirt) {
     for (int k = lane; k < Kpad; k += 32)
-      for (int s = 0; s < nsl; ++s) s0[s * plane + k] = __float2half_rn(0.0f);
+      for (int s = 0; s < nsl; ++s) s0[s * plane + k] = hz;
     if (lane == 0) inv_scale[warp] = 1.0f;
     return;
   }
   const double *c = Ca + ((size_t)i * nvirt + a) * NBA;
-  double mx = 0.0, ss = 0.0;
+  // pass 1: max |C| (integer compare of magnitudes) and sum of squares (FP32)
+  unsigned long long mxb = 0;
+  float ss = 0.0f;
   for (int k = lane; k < NBA; k += 32) {
-    const double v = c[k];
-    mx = fmax(mx, fabs(v));
-    ss += v * v;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(c[k]);
+    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+    mxb = mag > mxb ? mag : mxb;
+    const float f = bits_to_float_trunc(mag, 0);
+    ss = fmaf(f, f, ss);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, mxb, o);
+    mxb = other > mxb ? other : mxb;
     ss += __shfl_xor_sync(0xffffffffu, ss, o);
   }
+  const double mx = __longlong_as_double((long long)mxb);
   int e = 0;
   if (mx > 0.0) {
-    const double lim = fmin(255.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / sqrt(ss));
-    e = (int)floor(log2(lim));
+    // float truncation of the squares underestimates ||C||^2 by < 2^-21
+    // relative; the exact integer check below keeps the exactness guarantee
+    const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
+    const double lim = fmin(255.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / nrm);
+    e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
     e = max(-100, min(100, e));
   }
   for (int attempt = 0; attempt < 64; ++attempt) {
-    const double sc = ldexp(1.0, e);
-    double n2 = 0.0;
+    int n2 = 0;  // sum of S0^2: <= 4096*65536 per column, fits int32 with margin for 2^24 test
     for (int k = lane; k < Kpad; k += 32) {
-      __half h0 = __float2half_rn(0.0f), h1 = h0, h2 = h0;
+      __half h0 = hz, h1 = hz, h2 = hz;
       if (k < NBA) {
-        const double x = c[k] * sc;
-        const double q = rint(x);
-        const double r = x - q;  // exact
-        h0 = __double2half(q);   // integer |q| <= 256: exact
-        h1 = __double2half(r);
-        h2 = __double2half(r - (double)__half2float(h1));
-        n2 += q * q;
+        float xh, xl;
+        split_double(c[k], e, xh, xl);
+        const float q = rintf(xh);
+        const float r = (xh - q) + xl;  // xh - q exact
+        h0 = __float2half_rn(q);        // integer |q| <= 256: exact
+        h1 = __float2half_rn(r);
+        h2 = __float2half_rn(r - __half2float(h1));
+        const int qi = (int)q;
+        n2 += qi * qi;
       }
       s0[k] = h0;
       if (nsl > 1) s0[plane + k] = h1;
@@ -236,7 +280,7 @@ __global__ void slice_kernel(const double *__restrict__ Ca, int NBA, int nvirt, 
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
-    if (n2 <= 16777216.0) break;  // ||S0||^2 <= 2^24: L0 accumulation exact
+    if (n2 <= 16777216) break;  // ||S0||^2 <= 2^24: L0 accumulation exact
     --e;
   }
   if (lane == 0) inv_scale[warp] = ldexpf(1.0f, -e);
@@ -636,9 +680,9 @@ int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
   if (timed) RIMP2_CK(cudaEventRecord(ev[2], s));
 
   RIMP2_CK(cudaMemsetAsync(a.Epair, 0, sizeof(double) * (size_t)a.nocc * a.nocc, s));
-  pair_reduce_kernel<<<npairs, 256, 0, s>>>(part.as<double>(), ntp, pairs.as<int>(), npairs, a.nocc,
-                                            a.Epair);
-  total_reduce_kernel<<<1, 32, 0, s>>>(a.Epair, a.nocc, a.Etot);
+  pair_reduce_kernel<<<(npairs + 7) / 8, 256, 0, s>>>(part.as<double>(), ntp, pairs.as<int>(),
+                                                     npairs, a.nocc, a.Epair);
+  total_reduce_kernel<<<1, 1024, 0, s>>>(a.Epair, a.nocc, a.Etot);
   count_launch(2);
   RIMP2_CK(cudaGetLastError());
   if (timed) {
