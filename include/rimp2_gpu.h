@@ -154,6 +154,21 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
  * (the per-shape-bucket choice that holds the energy error within 1e-7). */
 int rimp2_split_nslices(int nvirt, int nocc, int NBA);
 
+/* FP64 pair and total energies like rimp2_energy_dev(..., RIMP2_PREC_FP64),
+ * for callers that cannot allocate device memory when they call: it uses no
+ * cudaMalloc/cudaFree or allocating library routine, only a fixed 16 MiB
+ * device array inside this library (held on every GPU that loads it until
+ * the process exits).  Fragments whose pair list plus per-tile partials
+ * exceed it (8*npairs*(ceil(nvirt/64)(ceil(nvirt/64)+1)/2 + 1) bytes,
+ * npairs = nocc(nocc+1)/2) get RIMP2_ERR_ARG.  stream NULL = the default
+ * stream.  Calls share the array: calls that overlap on the GPU race.  The
+ * first call on a device looks the array up and should precede any stream
+ * capture.  No counterpart in the reference (its GPU driver allocates through
+ * OpenACC data regions, RIMP2.GPU.F90:107). */
+int rimp2_energy_fp64_noalloc_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
+                                  const double *dEVocc, const double *dEVvirt, double *dEpair,
+                                  double *dEtot, void *stream);
+
 /* Split form with an explicit slice count (1 = S0+R1, 2 = S0+R1+R2). */
 int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
                            const double *dEVocc, const double *dEVvirt, double *dEpair,

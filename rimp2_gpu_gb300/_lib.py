@@ -48,6 +48,8 @@ SIGNATURES = {
                          C.c_int),
     "rimp2_energy_split_dev": ([C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int, _vp],
                                C.c_int),
+    "rimp2_energy_fp64_noalloc_dev": ([C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+                                      C.c_int),
     "rimp2_split_nslices": ([C.c_int, C.c_int, C.c_int], C.c_int),
     "rimp2_energy_batched": ([_ip, _ip, _ip, _ip, _dp, _llp, _dp, _llp, _dp, _llp, _dp, _llp, _dp,
                               _ip], C.c_int),

@@ -100,6 +100,9 @@ struct PlainEnergyArgs {
 };
 int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s);
 int probe_fp64_peak(double *tflops, cudaStream_t s);
+void plain_energy_scratch_sizes(int nvirt, int nocc, long long *npairs, long long *nitems);
+int plain_energy_f64_scratch(const PlainEnergyArgs &a, int *pairs_scratch, double *part_scratch,
+                             cudaStream_t s);
 
 // ---- split-precision tcgen05 path (split_kernels.cu) ---------------------------
 struct SplitEnergyArgs {

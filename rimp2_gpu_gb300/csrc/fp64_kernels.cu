@@ -412,6 +412,36 @@ int launch_gemm_f64(const GemmDesc &g, cudaStream_t s) {
   return RIMP2_OK;
 }
 
+// Same launches as plain_energy_f64, with the pair list and the per-item
+// partials in caller-provided device scratch instead of stream-ordered
+// allocations.  pairs_scratch holds 2*npairs ints, part_scratch
+// npairs*ntp doubles (plain_energy_scratch_sizes gives both).
+void plain_energy_scratch_sizes(int nvirt, int nocc, long long *npairs, long long *nitems) {
+  const int ntile = (nvirt + TM - 1) / TM;
+  const long long ntp = (long long)ntile * (ntile + 1) / 2;
+  *npairs = (long long)nocc * (nocc + 1) / 2;
+  *nitems = *npairs * ntp;
+}
+
+int plain_energy_f64_scratch(const PlainEnergyArgs &a, int *pairs_scratch, double *part_scratch,
+                             cudaStream_t s) {
+  const int ntile = (a.nvirt + TM - 1) / TM;
+  const int ntp = ntile * (ntile + 1) / 2;
+  const int npairs = a.nocc * (a.nocc + 1) / 2;
+  const long long nitems = (long long)npairs * ntp;
+  make_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(a.nocc, pairs_scratch);
+  RIMP2_CK(cudaMemsetAsync(a.Epair, 0, sizeof(double) * (size_t)a.nocc * a.nocc, s));
+  plain_energy_kernel<<<(unsigned)nitems, NTHR, 0, s>>>(a.Ca, a.NBA, a.nvirt, a.nocc, a.eo, a.ev,
+                                                        pairs_scratch, ntile, part_scratch,
+                                                        a.tamp);
+  pair_reduce_kernel<<<(npairs + 7) / 8, 256, 0, s>>>(part_scratch, ntp, pairs_scratch, npairs,
+                                                     a.nocc, a.Epair);
+  total_reduce_kernel<<<1, 1024, 0, s>>>(a.Epair, a.nocc, a.Etot);
+  count_launch(4);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
 int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s) {
   const int ntile = (a.nvirt + TM - 1) / TM;
   const int ntp = ntile * (ntile + 1) / 2;

@@ -1,0 +1,119 @@
+// noalloc.cu -- FP64 pair/total energy entry point that allocates nothing.
+//
+// Why: some callers cannot allocate device memory at the point where they
+// need an energy -- a Fortran/OpenACC host program that has already handed
+// (nearly) all device memory to its own data regions, code that runs while
+// another library owns the CUDA memory pool, or a caller that must not
+// trigger allocator work mid-computation.  For them the library keeps its
+// working memory for this one path in a fixed, file-scope device array that
+// exists from the moment the library's module is loaded until the process
+// exits (on every GPU that loads it).
+//
+// Limit: NOALLOC_SCRATCH_BYTES = 16 MiB, holding the (i<=j) pair list and one
+// FP64 partial energy per (pair, 64x64 tile pair) work item:
+//   8*npairs*ntp + 8*npairs (+alignment) <= 16 MiB,
+//   npairs = nocc(nocc+1)/2, ntp = t(t+1)/2, t = ceil(nvirt/64).
+// nocc=128, nvirt=1024 needs 9.1 MB; larger fragments are rejected with
+// RIMP2_ERR_ARG and a message.
+//
+// Contract: every call shares the one array and it keeps the last call's
+// contents; each launch writes every scratch element it later reads (pair
+// list, partials), so nothing needs clearing between calls.  Calls whose
+// work overlaps on the GPU (different streams, or different host threads on
+// one device) race on the array: serialise them.  The first call on a device
+// looks up the array's device address (cudaGetSymbolAddress) with that device
+// current; make that first call before any stream capture.
+#include <mutex>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 16u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+static void *g_scratch_addr[kMaxDevices] = {};
+static std::mutex g_scratch_mu;
+
+// Device address of the scratch array on the current device (set up once per
+// device).  The name g_noalloc_scratch is only a host-side handle; kernels
+// must be given this address, never the symbol itself.
+int scratch_address(void **out) {
+  int dev = 0;
+  RIMP2_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    rimp2::set_error("rimp2_energy_fp64_noalloc_dev: device index %d out of range", dev);
+    return RIMP2_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      rimp2::set_error("cudaGetSymbolAddress(scratch) failed on device %d: %s", dev,
+                       cudaGetErrorString(e));
+      return RIMP2_ERR_CUDA;
+    }
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return RIMP2_OK;
+}
+
+// Device check without the library's lazily allocated state.
+int check_device_noalloc() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    (void)cudaGetLastError();
+    rimp2::set_error("no CUDA device available; this library has no CPU path");
+    return RIMP2_ERR_NODEV;
+  }
+  int dev = 0, major = 0, minor = 0;
+  RIMP2_CK(cudaGetDevice(&dev));
+  RIMP2_CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+  RIMP2_CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+  if (!(major == 10 && minor == 3)) {
+    rimp2::set_error("device is sm_%d%d; this library is built for sm_103a only", major, minor);
+    return RIMP2_ERR_NODEV;
+  }
+  return RIMP2_OK;
+}
+
+}  // namespace
+
+extern "C" int rimp2_energy_fp64_noalloc_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
+                                             const double *dEVocc, const double *dEVvirt,
+                                             double *dEpair, double *dEtot, void *stream) {
+  rimp2::clear_error();
+  RIMP2_REQ(nvirt > 0 && nocc > 0 && NBA > 0, "rimp2_energy_fp64_noalloc_dev: bad dims");
+  RIMP2_REQ(dCalpha && dEVocc && dEVvirt && dEpair && dEtot,
+            "rimp2_energy_fp64_noalloc_dev: null array");
+  long long npairs = 0, nitems = 0;
+  rimp2::plain_energy_scratch_sizes(nvirt, nocc, &npairs, &nitems);
+  const size_t pairs_bytes = ((size_t)(2 * npairs) * sizeof(int) + 255) & ~(size_t)255;
+  const size_t need = pairs_bytes + (size_t)nitems * sizeof(double);
+  RIMP2_REQ(nitems <= 2147483647LL && need <= NOALLOC_SCRATCH_BYTES,
+            "rimp2_energy_fp64_noalloc_dev: fragment nocc=%d nvirt=%d needs %zu bytes of scratch, "
+            "above the fixed %zu-byte limit of this allocation-free entry point",
+            nocc, nvirt, need, NOALLOC_SCRATCH_BYTES);
+  RIMP2_TRY(check_device_noalloc());
+  void *base = nullptr;
+  RIMP2_TRY(scratch_address(&base));
+  rimp2::PlainEnergyArgs a;
+  a.Ca = dCalpha;
+  a.NBA = NBA;
+  a.nvirt = nvirt;
+  a.nocc = nocc;
+  a.eo = dEVocc;
+  a.ev = dEVvirt;
+  a.Epair = dEpair;
+  a.Etot = dEtot;
+  a.tamp = nullptr;
+  a.pairs = nullptr;
+  a.npairs = 0;
+  int *pairs = static_cast<int *>(base);
+  double *part = reinterpret_cast<double *>(static_cast<unsigned char *>(base) + pairs_bytes);
+  return rimp2::plain_energy_f64_scratch(a, pairs, part, (cudaStream_t)stream);
+}

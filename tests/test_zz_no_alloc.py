@@ -1,0 +1,64 @@
+"""The allocation-free FP64 energy entry point, through the C-ABI.
+
+Callers such as a Fortran/OpenACC driver that already owns the device memory
+cannot let the library allocate; rimp2_energy_fp64_noalloc_dev works out of a
+fixed device array instead.  Its energies must match the regular FP64 entry
+point (same 1e-11 relative tolerance as the FP64 parity tests) on two calls
+in a row, the second reusing the array left by the first.  Collected last so
+that a failure here never hides the other tests.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a).ravel(order="F")).cuda()
+
+
+def test_noalloc_matches_regular_entry_point_twice():
+    import torch
+    from rimp2_gpu_gb300 import _lib, api
+    L = _lib.lib()
+    cases = [(7, 96, 200, 41), (4, 130, 77, 42)]
+    for nocc, nvirt, NBA, seed in cases:
+        Ca, eo, ev = O.gen_fragment(seed, nocc, nvirt, NBA)
+        dC = _dev(Ca.reshape(-1, order="F"))
+        deo, dev = _dev(eo), _dev(ev)
+        ref_E = torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda")
+        ref_T = torch.zeros(1, dtype=torch.float64, device="cuda")
+        api.energy_dev(nvirt, nocc, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(),
+                       ref_E.data_ptr(), ref_T.data_ptr(), precision=api.PREC_FP64)
+        torch.cuda.synchronize()
+        Er = ref_E.cpu().numpy()
+        Tr = ref_T.item()
+        for call in range(2):
+            dE = torch.full((nocc * nocc,), np.nan, dtype=torch.float64, device="cuda")
+            dT = torch.full((1,), np.nan, dtype=torch.float64, device="cuda")
+            st = L.rimp2_energy_fp64_noalloc_dev(nvirt, nocc, NBA, dC.data_ptr(), deo.data_ptr(),
+                                                 dev.data_ptr(), dE.data_ptr(), dT.data_ptr(),
+                                                 None)
+            assert st == 0, L.rimp2_last_error_string()
+            torch.cuda.synchronize()
+            E = dE.cpu().numpy()
+            rel = np.abs(E - Er) / np.abs(Er)
+            assert rel.max() <= 1e-11, (call, rel.max())
+            assert abs(dT.item() - Tr) <= 1e-11 * abs(Tr), call
+
+
+def test_noalloc_rejects_fragments_above_its_limit():
+    import torch
+    from rimp2_gpu_gb300 import _lib
+    L = _lib.lib()
+    d = torch.zeros(8, dtype=torch.float64, device="cuda")
+    p = d.data_ptr()
+    # nocc=512, nvirt=2048: 131328 pairs x 528 tile pairs of partials >> 16 MiB
+    st = L.rimp2_energy_fp64_noalloc_dev(2048, 512, 64, p, p, p, p, p, None)
+    assert st == 1
+    assert b"limit" in L.rimp2_last_error_string()
