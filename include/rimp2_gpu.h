@@ -184,6 +184,27 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
                          double *Epair, const long long *epair_off, double *Etot,
                          const int *precision);
 
+/* Batched split-precision energies of many fragments of uneven size, all
+ * resident on the device, in ONE persistent launch per slice-count group:
+ * a device-side queue of (fragment, pair i<=j, tile pair) work items ordered
+ * heaviest fragment first, drained by one CTA per SM.  With use_graph != 0
+ * the whole evaluation (slicing, energy kernel, reductions) is captured once
+ * as a CUDA graph and every execute is one graph launch.  nslices may be NULL
+ * (per-fragment choice from the shape-bucket table).  The plan keeps its
+ * workspace until destroyed and reads the fragment pointers at every
+ * execute.  No counterpart in the reference (one fragment per driver run,
+ * RIMP2.F90:36-377). */
+int rimp2_batch_plan_create(void **plan, int nfrag, const int *nocc, const int *nvirt,
+                            const int *NBA, const double *const *dCalpha,
+                            const double *const *dEVocc, const double *const *dEVvirt,
+                            double *const *dEpair, double *const *dEtot, const int *nslices,
+                            int use_graph, void *stream);
+int rimp2_batch_plan_execute(void *plan, void *stream);
+int rimp2_batch_plan_destroy(void *plan);
+/* Shape-bucket table of the split form: fragments with nvirt >= nvirt_min[k]
+ * (largest such k) use nslices[k] residual slices (autotuner output). */
+int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices);
+
 /* ---- synthetic fragments (benchmark / test inputs; no counterpart in the
  * reference, whose fixtures are constants written by generate.F90) --------
  * Seeded Philox4x32-10 + Box-Muller on the device:

@@ -55,6 +55,12 @@ SIGNATURES = {
                               _ip], C.c_int),
     "rimp2_gen_fragment_dev": ([C.c_ulonglong, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp],
                                C.c_int),
+    "rimp2_batch_plan_create": ([C.POINTER(_vp), C.c_int, _ip, _ip, _ip, C.POINTER(_vp),
+                                 C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
+                                 _ip, C.c_int, _vp], C.c_int),
+    "rimp2_batch_plan_execute": ([_vp, _vp], C.c_int),
+    "rimp2_batch_plan_destroy": ([_vp], C.c_int),
+    "rimp2_set_split_buckets": ([C.c_int, _ip, _ip], C.c_int),
     "rimp2_calpha_from_ao": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp], C.c_int),
 }
 

@@ -189,6 +189,53 @@ def gen_fragment_dev(seed, nocc, nvirt, NBA, dCalpha=0, dEVocc=0, dEVvirt=0, str
          dEVvirt or None, stream or None)
 
 
+class BatchPlan:
+    """Batched split-precision energies of many device-resident fragments:
+    one persistent launch per slice-count group draining a device work
+    queue, optionally captured once as a CUDA graph (C-ABI
+    rimp2_batch_plan_*).  ``frags`` is a list of
+    (nocc, nvirt, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot) with device
+    addresses; outputs are written at every ``execute``."""
+
+    def __init__(self, frags, nslices=None, graph=True, stream=0):
+        n = len(frags)
+        ia = lambda k: (C.c_int * n)(*[int(f[k]) for f in frags])  # noqa: E731
+        pa = lambda k: (C.c_void_p * n)(*[int(f[k]) for f in frags])  # noqa: E731
+        self._keep = [ia(0), ia(1), ia(2), pa(3), pa(4), pa(5), pa(6), pa(7)]
+        ns = (C.c_int * n)(*nslices) if nslices is not None else None
+        self._keep.append(ns)
+        self._plan = C.c_void_p()
+        # C order: (plan, nfrag, nocc[], nvirt[], NBA[], Calpha[], EVocc[], EVvirt[], Epair[],
+        # Etot[], nslices[], use_graph, stream)
+        call("rimp2_batch_plan_create", C.byref(self._plan), n, self._keep[0], self._keep[1],
+             self._keep[2], self._keep[3], self._keep[4], self._keep[5], self._keep[6],
+             self._keep[7], ns, 1 if graph else 0, stream or None)
+
+    def execute(self, stream=0):
+        call("rimp2_batch_plan_execute", self._plan, stream or None)
+
+    def close(self):
+        if self._plan:
+            call("rimp2_batch_plan_destroy", self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_split_buckets(nvirt_min, nslices):
+    """Install a shape-bucket table for the split form's slice count."""
+    n = len(nvirt_min)
+    call("rimp2_set_split_buckets", n, (C.c_int * n)(*nvirt_min), (C.c_int * n)(*nslices))
+
+
+def split_nslices(nvirt, nocc, NBA):
+    return lib().rimp2_split_nslices(nvirt, nocc, NBA)
+
+
 def calpha_from_ao(NBA, nbas, nocc, nvirt, ao, V, Cmo):
     """Calpha(NBA,nvirt,nocc) from AO three-centre integrals, metric and MO
     coefficients (FP64 Cholesky + triangular solve on the GPU)."""

@@ -7,6 +7,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
 
@@ -692,13 +694,79 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
   return plain_energy_f64(a, s);
 }
 
+// Residual slices per element by shape bucket, chosen so that the pair and
+// total energies stay within 1e-7 relative of FP64: one residual slice
+// suffices once the pair sums average over enough (a,b) terms, small
+// fragments get two.  Buckets are keyed by nvirt (the (a,b) count per pair);
+// the autotuner (rimp2_gpu_gb300/autotune.py) may replace the table.
+static std::vector<std::pair<int, int>> g_buckets = {{0, 2}, {256, 1}};
+static std::mutex g_bucket_mu;
+
 int rimp2_split_nslices(int nvirt, int nocc, int NBA) {
-  // Residual slices per element chosen so that the pair and total energies
-  // stay within 1e-7 relative of FP64: one residual slice suffices once the
-  // pair sums average over enough (a,b) terms, small fragments get two.
   (void)nocc;
   (void)NBA;
-  return nvirt >= 256 ? 1 : 2;
+  std::lock_guard<std::mutex> lk(g_bucket_mu);
+  int ns = 2;
+  for (auto &b : g_buckets)
+    if (nvirt >= b.first) ns = b.second;
+  return ns;
+}
+
+int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices) {
+  clear_error();
+  RIMP2_REQ(n > 0 && n <= 64 && nvirt_min && nslices, "rimp2_set_split_buckets: bad table");
+  std::vector<std::pair<int, int>> t;
+  for (int k = 0; k < n; ++k) {
+    RIMP2_REQ(nslices[k] == 1 || nslices[k] == 2, "rimp2_set_split_buckets: nslices must be 1 or 2");
+    RIMP2_REQ(k == 0 || nvirt_min[k] > nvirt_min[k - 1],
+              "rimp2_set_split_buckets: nvirt_min must increase");
+    t.push_back({nvirt_min[k], nslices[k]});
+  }
+  std::lock_guard<std::mutex> lk(g_bucket_mu);
+  g_buckets = t;
+  return RIMP2_OK;
+}
+
+int rimp2_batch_plan_create(void **plan, int nfrag, const int *nocc, const int *nvirt,
+                            const int *NBA, const double *const *dCalpha,
+                            const double *const *dEVocc, const double *const *dEVvirt,
+                            double *const *dEpair, double *const *dEtot, const int *nslices,
+                            int use_graph, void *stream) {
+  clear_error();
+  RIMP2_REQ(plan, "rimp2_batch_plan_create: null plan");
+  *plan = nullptr;
+  RIMP2_REQ(nfrag > 0 && nocc && nvirt && NBA && dCalpha && dEVocc && dEVvirt && dEpair && dEtot,
+            "rimp2_batch_plan_create: null argument");
+  std::vector<int> ns(nfrag);
+  for (int f = 0; f < nfrag; ++f) {
+    RIMP2_REQ(nocc[f] > 0 && nvirt[f] > 0 && NBA[f] > 0 && nocc[f] < 65536,
+              "rimp2_batch_plan_create: bad dims in fragment %d", f);
+    RIMP2_REQ(dCalpha[f] && dEVocc[f] && dEVvirt[f] && dEpair[f] && dEtot[f],
+              "rimp2_batch_plan_create: null device pointer in fragment %d", f);
+    ns[f] = nslices ? nslices[f] : rimp2_split_nslices(nvirt[f], nocc[f], NBA[f]);
+    RIMP2_REQ(ns[f] == 1 || ns[f] == 2, "rimp2_batch_plan_create: nslices must be 1 or 2");
+  }
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  SplitPlan *P = nullptr;
+  RIMP2_TRY(split_plan_create(&P, nfrag, nocc, nvirt, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot,
+                              ns.data(), use_graph != 0, s));
+  *plan = P;
+  return RIMP2_OK;
+}
+
+int rimp2_batch_plan_execute(void *plan, void *stream) {
+  clear_error();
+  RIMP2_REQ(plan, "rimp2_batch_plan_execute: null plan");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  return split_plan_execute((SplitPlan *)plan, s);
+}
+
+int rimp2_batch_plan_destroy(void *plan) {
+  clear_error();
+  if (plan) split_plan_destroy((SplitPlan *)plan);
+  return RIMP2_OK;
 }
 
 int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
@@ -764,12 +832,80 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
             "rimp2_energy_batched: null argument");
   for (int f = 0; f < *nfrag; ++f)
     RIMP2_REQ(nocc[f] > 0 && nvirt[f] > 0 && NBA[f] > 0, "rimp2_energy_batched: bad dims in %d", f);
-  for (int f = 0; f < *nfrag; ++f) {
-    int rc = rimp2_energy(&nvirt[f], &nocc[f], &NBA[f], Calpha + calpha_off[f], EVocc + eo_off[f],
-                          EVvirt + ev_off[f], Epair + epair_off[f], Etot + f, nullptr, precision);
-    if (rc != RIMP2_OK) return rc;
+  RIMP2_REQ(*precision == RIMP2_PREC_FP64 || *precision == RIMP2_PREC_SPLIT,
+            "rimp2_energy_batched: bad precision");
+  const int nf = *nfrag;
+  if (nf == 0) return RIMP2_OK;
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  // one device copy of every fragment (inputs are in HBM together; the
+  // split form then runs the whole batch as one persistent launch)
+  size_t nca = 0, neo = 0, nev = 0, nep = 0;
+  for (int f = 0; f < nf; ++f) {
+    nca += (size_t)NBA[f] * nvirt[f] * nocc[f];
+    neo += nocc[f];
+    nev += nvirt[f];
+    nep += (size_t)nocc[f] * nocc[f];
   }
-  return RIMP2_OK;
+  DevBuf dC, deo, dev, dE, dT;
+  RIMP2_TRY(dalloc(dC, nca, s));
+  RIMP2_TRY(dalloc(deo, neo, s));
+  RIMP2_TRY(dalloc(dev, nev, s));
+  RIMP2_TRY(dalloc(dE, nep, s));
+  RIMP2_TRY(dalloc(dT, nf, s));
+  std::vector<const double *> pc(nf), peo(nf), pev(nf);
+  std::vector<double *> pE(nf), pT(nf);
+  size_t oc = 0, oo = 0, ov = 0, oe = 0;
+  for (int f = 0; f < nf; ++f) {
+    const size_t n = (size_t)NBA[f] * nvirt[f] * nocc[f];
+    RIMP2_CK(cudaMemcpyAsync(dC.as<double>() + oc, Calpha + calpha_off[f], n * 8,
+                             cudaMemcpyHostToDevice, s));
+    RIMP2_CK(cudaMemcpyAsync(deo.as<double>() + oo, EVocc + eo_off[f], (size_t)nocc[f] * 8,
+                             cudaMemcpyHostToDevice, s));
+    RIMP2_CK(cudaMemcpyAsync(dev.as<double>() + ov, EVvirt + ev_off[f], (size_t)nvirt[f] * 8,
+                             cudaMemcpyHostToDevice, s));
+    pc[f] = dC.as<double>() + oc;
+    peo[f] = deo.as<double>() + oo;
+    pev[f] = dev.as<double>() + ov;
+    pE[f] = dE.as<double>() + oe;
+    pT[f] = dT.as<double>() + f;
+    oc += n;
+    oo += nocc[f];
+    ov += nvirt[f];
+    oe += (size_t)nocc[f] * nocc[f];
+  }
+  if (*precision == RIMP2_PREC_SPLIT) {
+    void *plan = nullptr;
+    RIMP2_TRY(rimp2_batch_plan_create(&plan, nf, nocc, nvirt, NBA, pc.data(), peo.data(),
+                                      pev.data(), pE.data(), pT.data(), nullptr, 0, s));
+    int rc = rimp2_batch_plan_execute(plan, s);
+    rimp2_batch_plan_destroy(plan);
+    RIMP2_TRY(rc);
+  } else {
+    for (int f = 0; f < nf; ++f) {
+      PlainEnergyArgs a;
+      a.Ca = pc[f];
+      a.NBA = NBA[f];
+      a.nvirt = nvirt[f];
+      a.nocc = nocc[f];
+      a.eo = peo[f];
+      a.ev = pev[f];
+      a.Epair = pE[f];
+      a.Etot = pT[f];
+      a.tamp = nullptr;
+      a.pairs = nullptr;
+      a.npairs = 0;
+      RIMP2_TRY(plain_energy_f64(a, s));
+    }
+  }
+  oe = 0;
+  for (int f = 0; f < nf; ++f) {
+    RIMP2_CK(cudaMemcpyAsync(Epair + epair_off[f], dE.as<double>() + oe,
+                             (size_t)nocc[f] * nocc[f] * 8, cudaMemcpyDeviceToHost, s));
+    oe += (size_t)nocc[f] * nocc[f];
+  }
+  RIMP2_CK(cudaMemcpyAsync(Etot, dT.p, (size_t)nf * 8, cudaMemcpyDeviceToHost, s));
+  return finish(s);
 }
 
 int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc, const int *nvirt,

@@ -113,6 +113,13 @@ struct SplitEnergyArgs {
   int nslices;  // residual slices per element (1 or 2)
 };
 int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel);
+struct SplitPlan;
+int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nvirt, const int *NBA,
+                      const double *const *Ca, const double *const *eo, const double *const *ev,
+                      double *const *Epair, double *const *Etot, const int *nslices, bool graph,
+                      cudaStream_t s);
+int split_plan_execute(SplitPlan *P, cudaStream_t s);
+void split_plan_destroy(SplitPlan *P);
 bool split_supported();
 
 }  // namespace rimp2

@@ -33,7 +33,10 @@
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 
@@ -215,25 +218,67 @@ __device__ __forceinline__ void split_double(double c, int e, float &xh, float &
   if (mag == 0 || ex < -126) xl = 0.0f;
 }
 
-__global__ void slice_kernel(const double *__restrict__ Ca, int NBA, int nvirt, int nocc,
-                             int nvpad, int Kpad, int nsl, __half *__restrict__ slices,
-                             float *__restrict__ inv_scale) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// One fragment of a batch: sizes, where its data lives, where its slices,
+// scales, work items and pair energies go.
+struct FragDesc {
+  int nocc, nvirt, nvpad, NBA;
+  int nks;              // K chunks of 64
+  int ntp;              // tile pairs A<=B
+  int ncol;             // nocc * nvpad
+  int eo_off, ev_off;   // into eo2 / ev2
+  int pair_base;        // first global pair index
+  long long row_base;   // first 64-wide slice row (per slice plane)
+  long long col_base;   // first inverse-scale index
+  long long item_base;  // first work item
+  const double *Ca, *eo, *ev;
+  double *Epair, *Etot;
+};
+
+__device__ __forceinline__ int find_frag_item(const FragDesc *fr, int nfrag, long long x) {
+  int lo = 0, hi = nfrag - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (fr[mid].item_base <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void decode_pair(int p, int &i, int &j) {
+  int jj = (int)((sqrtf(8.0f * p + 1.0f) - 1.0f) * 0.5f);
+  while ((jj + 1) * (jj + 2) / 2 <= p) ++jj;
+  while (jj * (jj + 1) / 2 > p) --jj;
+  j = jj;
+  i = p - jj * (jj + 1) / 2;
+}
+
+// Slices of every fragment: slice plane s, fragment f, K chunk kc, column c
+// live at row (row_base_f + kc*ncol_f + c) of 64 FP16, i.e. one 2D-boxable
+// K-chunk-major layout shared by all fragments (one tensor map per batch).
+// grid.y = fragment, one warp per column.
+__global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, long long plane,
+                                   __half *__restrict__ slices, float *__restrict__ inv_scale) {
+  const FragDesc &F = fr[blockIdx.y];
+  const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  const int ncol = nvpad * nocc;
-  if (warp >= ncol) return;
-  const int a = warp % nvpad, i = warp / nvpad;
-  const size_t plane = (size_t)ncol * Kpad;
-  __half *s0 = slices + (size_t)warp * Kpad;
+  if (col >= F.ncol) return;
+  const int a = col % F.nvpad, i = col / F.nvpad;
+  const int Kpad = F.nks * 64;
   const __half hz = __float2half_rn(0.0f);
-  if (a >= nvirt) {
-    for (int k = lane; k < Kpad; k += 32)
-      for (int s = 0; s < nsl; ++s) s0[s * plane + k] = hz;
-    if (lane == 0) inv_scale[warp] = 1.0f;
+  __half *out = slices + (size_t)(F.row_base + col) * 64;
+  const size_t kstride = (size_t)F.ncol * 64;  // next K chunk of the same column
+  if (a >= F.nvirt) {
+    for (int k = lane; k < Kpad; k += 32) {
+      const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
+      for (int sl = 0; sl < nsl; ++sl) out[sl * plane + o] = hz;
+    }
+    if (lane == 0) inv_scale[F.col_base + col] = 1.0f;
     return;
   }
-  const double *c = Ca + ((size_t)i * nvirt + a) * NBA;
-  // pass 1: max |C| (integer compare of magnitudes) and sum of squares (FP32)
+  const int NBA = F.NBA;
+  const double *c = F.Ca + ((size_t)i * F.nvirt + a) * NBA;
   unsigned long long mxb = 0;
   float ss = 0.0f;
   for (int k = lane; k < NBA; k += 32) {
@@ -260,7 +305,7 @@ __global__ void slice_kernel(const double *__restrict__ Ca, int NBA, int nvirt, 
     e = max(-100, min(100, e));
   }
   for (int attempt = 0; attempt < 64; ++attempt) {
-    int n2 = 0;  // sum of S0^2: <= 4096*65536 per column, fits int32 with margin for 2^24 test
+    int n2 = 0;  // sum of S0^2 (integers; <= 2^24 is the test)
     for (int k = lane; k < Kpad; k += 32) {
       __half h0 = hz, h1 = hz, h2 = hz;
       if (k < NBA) {
@@ -274,62 +319,79 @@ __global__ void slice_kernel(const double *__restrict__ Ca, int NBA, int nvirt, 
         const int qi = (int)q;
         n2 += qi * qi;
       }
-      s0[k] = h0;
-      if (nsl > 1) s0[plane + k] = h1;
-      if (nsl > 2) s0[2 * plane + k] = h2;
+      const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
+      out[o] = h0;
+      if (nsl > 1) out[plane + o] = h1;
+      if (nsl > 2) out[2 * plane + o] = h2;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
     if (n2 <= 16777216) break;  // ||S0||^2 <= 2^24: L0 accumulation exact
     --e;
   }
-  if (lane == 0) inv_scale[warp] = ldexpf(1.0f, -e);
+  if (lane == 0) inv_scale[F.col_base + col] = ldexpf(1.0f, -e);
 }
 
 // orbital energies as hi/lo float pairs (padded virtuals get a large value so
-// their denominators stay finite; their g is exactly zero)
-__global__ void eps_split_kernel(const double *eo, int nocc, const double *ev, int nvirt, int nvpad,
-                                 float2 *eo2, float2 *ev2) {
+// their denominators stay finite; their g is exactly zero). grid.y = fragment
+__global__ void eps_batch_kernel(const FragDesc *__restrict__ fr, float2 *eo2, float2 *ev2) {
+  const FragDesc &F = fr[blockIdx.y];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nocc) {
-    const float h = (float)eo[t];
-    eo2[t] = make_float2(h, (float)(eo[t] - (double)h));
-  }
-  if (t < nvpad) {
-    const double v = t < nvirt ? ev[t] : 1000.0;
+  if (t < F.nocc) {
+    const double v = F.eo[t];
     const float h = (float)v;
-    ev2[t] = make_float2(h, (float)(v - (double)h));
+    eo2[F.eo_off + t] = make_float2(h, (float)(v - (double)h));
+  }
+  if (t < F.nvpad) {
+    const double v = t < F.nvirt ? F.ev[t] : 1000.0;
+    const float h = (float)v;
+    ev2[F.ev_off + t] = make_float2(h, (float)(v - (double)h));
   }
 }
 
-// --------------------------------------------------------------------------
-// the persistent split-precision energy kernel
-// --------------------------------------------------------------------------
-struct SplitParams {
-  int nocc, nvpad, ntile, ntp, nks, nsl, npairs;
+// Work items in queue order: fragments are enumerated heaviest first (the
+// host orders the descriptors by K length), pairs j-major, tile pairs
+// B-major.  item = {fragment, i | j<<16, tA | tB<<16, item id}.
+__global__ void build_items_kernel(const FragDesc *__restrict__ fr, int nfrag, long long nitems,
+                                   int4 *__restrict__ items) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= nitems) return;
+  const int f = find_frag_item(fr, nfrag, t);
+  const FragDesc &F = fr[f];
+  const long long loc = t - F.item_base;
+  const int p = (int)(loc / F.ntp), q = (int)(loc % F.ntp);
+  int i, j, tA, tB;
+  decode_pair(p, i, j);
+  decode_tri(q, tA, tB);
+  items[t] = make_int4(f, i | (j << 16), tA | (tB << 16), (int)t);
+}
+
+struct BatchParams {
+  const FragDesc *frags;
+  const int4 *items;
   long long nitems;
-  const int *pairs;        // (i<=j) pair list
-  const float2 *eo2;       // [nocc]
-  const float2 *ev2;       // [nvpad]
-  const float *inv_scale;  // [nocc*nvpad]
+  unsigned int *queue;     // next item counter (reset per launch)
+  const float2 *eo2, *ev2;
+  const float *inv_scale;
   double *part;            // [nitems]
-  int *err;                // error word
+  int *err;
 };
+
+constexpr int IQ = 4;  // item ring depth between the producer and the consumers
 
 template <int NSL, int NSTAGE>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    split_energy_kernel(const __grid_constant__ CUtensorMap tmap, SplitParams P) {
+    split_batch_kernel(const __grid_constant__ CUtensorMap tmap, BatchParams P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  // 1024-aligned operand stages
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int STAGE_BYTES = NSL * 2 * PANEL_BYTES;
   uint8_t *stages = base;
   uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
-  // bars: full[NSTAGE], empty[NSTAGE], tmem_full, tmem_empty, drain
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NSTAGE + 3);
+  // bars: full[NSTAGE], empty[NSTAGE], tmem_full, tmem_empty, drain, item_full[IQ], item_empty[IQ]
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NSTAGE + 3 + 2 * IQ);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
-  float *red = (float *)(tmem_slot + 4);  // [4] epilogue warp partials (as double pairs)
-  double *redd = (double *)(((uintptr_t)(red) + 7) & ~(uintptr_t)7);
+  volatile int *item_q = (volatile int *)(tmem_slot + 2);  // [IQ]
+  double *redd = (double *)(((uintptr_t)(tmem_slot + 2 + IQ) + 7) & ~(uintptr_t)7);  // [4]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(&bars[0]);
@@ -337,6 +399,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const uint32_t tfull = smem_u32(&bars[2 * NSTAGE]);
   const uint32_t tempty = smem_u32(&bars[2 * NSTAGE + 1]);
   const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 2]);
+  const uint32_t ifull0 = smem_u32(&bars[2 * NSTAGE + 3]);
+  const uint32_t iempty0 = smem_u32(&bars[2 * NSTAGE + 3 + IQ]);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
@@ -346,6 +410,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     mbar_init(tfull, 1);
     mbar_init(tempty, 4);
     mbar_init(drain, 1);
+    for (int s = 0; s < IQ; ++s) {
+      mbar_init(ifull0 + 8 * s, 1);
+      mbar_init(iempty0 + 8 * s, 5);  // MMA issuer + 4 epilogue warps
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmap) : "memory");
@@ -361,27 +429,33 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  const long long nitems = P.nitems;
-  const int ntp = P.ntp, nks = P.nks, nvpad = P.nvpad;
-
   if (warp == 0) {
     // ------------------------------ TMA producer ------------------------------
     if (lane == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
+      int stage = 0, islot = 0;
+      uint32_t phase = 0, iphase = 0;
       int armed[NSTAGE];
       for (int s = 0; s < NSTAGE; ++s) armed[s] = -1;
       bool ok = true;
-      for (long long it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
-        const int p = (int)(it / ntp), q = (int)(it % ntp);
-        int tA, tB;
-        decode_tri(q, tA, tB);
-        const int i = P.pairs[2 * p], j = P.pairs[2 * p + 1];
+      while (ok) {
+        if (!mbar_wait(iempty0 + 8 * islot, iphase ^ 1, abort_flag, P.err, 5)) break;
+        const unsigned int id = atomicAdd(P.queue, 1u);
+        const int qidx = (long long)id < P.nitems ? (int)id : -1;
+        item_q[islot] = qidx;
+        mbar_arrive(ifull0 + 8 * islot);
+        if (++islot == IQ) {
+          islot = 0;
+          iphase ^= 1;
+        }
+        if (qidx < 0) break;
+        const int4 it = P.items[qidx];
+        const FragDesc &F = P.frags[it.x];
+        const int i = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
         const int ntiles = (i == j) ? 1 : 2;
         for (int t = 0; t < ntiles && ok; ++t) {
-          const int colA = (t == 0 ? i : j) * nvpad + tA * TILE;
-          const int colB = (t == 0 ? j : i) * nvpad + tB * TILE;
-          for (int ks = 0; ks < nks; ++ks) {
+          const int colA = (t == 0 ? i : j) * F.nvpad + tA * TILE;
+          const int colB = (t == 0 ? j : i) * F.nvpad + tB * TILE;
+          for (int kc = 0; kc < F.nks; ++kc) {
             if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err, 1)) {
               ok = false;
               break;
@@ -390,10 +464,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             mbar_expect_tx(fb, STAGE_BYTES);
             armed[stage] = (int)phase;
             const uint32_t dst = smem_u32(stages + stage * STAGE_BYTES);
+            const int rowk = (int)(F.row_base + (long long)kc * F.ncol);
 #pragma unroll
             for (int sl = 0; sl < NSL; ++sl) {
-              tma_load_3d(dst + (2 * sl) * PANEL_BYTES, &tmap, fb, ks * KSTEP, colA, sl);
-              tma_load_3d(dst + (2 * sl + 1) * PANEL_BYTES, &tmap, fb, ks * KSTEP, colB, sl);
+              tma_load_3d(dst + (2 * sl) * PANEL_BYTES, &tmap, fb, 0, rowk + colA, sl);
+              tma_load_3d(dst + (2 * sl + 1) * PANEL_BYTES, &tmap, fb, 0, rowk + colB, sl);
             }
             if (++stage == NSTAGE) {
               stage = 0;
@@ -402,7 +477,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
         }
       }
-      if (!ok) {  // drain copies in flight before the CTA can exit
+      if (!ok || *abort_flag) {  // drain copies in flight before the CTA can exit
         for (int s = 0; s < NSTAGE; ++s) {
           if (armed[s] < 0) continue;
           const long long t0 = clock64();
@@ -414,25 +489,31 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     // ------------------------------ MMA issuer --------------------------------
     if (lane == 0) {
-      int stage = 0;
-      uint32_t phase = 0;
+      int stage = 0, islot = 0;
+      uint32_t phase = 0, iphase = 0;
       bool ok = true;
       long long nloc = 0;
-      for (long long it = blockIdx.x; it < nitems && ok; it += gridDim.x, ++nloc) {
-        const int p = (int)(it / ntp);
-        const int i = P.pairs[2 * p], j = P.pairs[2 * p + 1];
+      while (ok) {
+        if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 6)) break;
+        const int qidx = item_q[islot];
+        mbar_arrive(iempty0 + 8 * islot);
+        if (++islot == IQ) {
+          islot = 0;
+          iphase ^= 1;
+        }
+        if (qidx < 0) break;
+        const int4 it = P.items[qidx];
+        const int nks = P.frags[it.x].nks;
+        const int i = it.y & 0xFFFF, j = it.y >> 16;
         const int ntiles = (i == j) ? 1 : 2;
         if (nloc > 0) {  // epilogue must have drained TMEM of the previous item
-          if (!mbar_wait(tempty, (uint32_t)((nloc - 1) & 1), abort_flag, P.err, 2)) {
-            ok = false;
-            break;
-          }
+          if (!mbar_wait(tempty, (uint32_t)((nloc - 1) & 1), abort_flag, P.err, 2)) break;
         }
         tc_fence_after();
         for (int t = 0; t < ntiles && ok; ++t) {
           const uint32_t dL0 = tmem + (uint32_t)(t * 2 * TILE);
           const uint32_t dL1 = dL0 + TILE;
-          for (int ks = 0; ks < nks; ++ks) {
+          for (int kc = 0; kc < nks; ++kc) {
             if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err, 3)) {
               ok = false;
               break;
@@ -446,7 +527,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint64_t b0 = smem_desc(sb + 1 * PANEL_BYTES + koff);
               const uint64_t a1 = smem_desc(sb + 2 * PANEL_BYTES + koff);
               const uint64_t b1 = smem_desc(sb + 3 * PANEL_BYTES + koff);
-              const uint32_t acc = (ks > 0 || k16 > 0) ? 1u : 0u;
+              const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
               mma_f16(dL0, a0, b0, acc);  // exact integer part
               mma_f16(dL1, a0, b1, acc);  // S0a R1b
               mma_f16(dL1, a1, b0, 1u);   // R1a S0b
@@ -465,7 +546,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
           }
         }
-        if (ok) mma_commit(tfull);  // accumulators of this item complete
+        if (!ok) break;
+        mma_commit(tfull);  // accumulators of this item complete
+        ++nloc;
       }
       // drain: all MMAs issued by this thread complete before TMEM is freed
       mma_commit(drain);
@@ -478,18 +561,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int ew = warp - 2;           // 0..3
     const int quad = warp & 3;         // TMEM lane quadrant this warp may access
     const int row = quad * 32 + lane;  // tile row = a offset
+    int islot = 0;
+    uint32_t iphase = 0;
     long long nloc = 0;
-    for (long long it = blockIdx.x; it < nitems; it += gridDim.x, ++nloc) {
-      const int p = (int)(it / ntp), q = (int)(it % ntp);
-      int tA, tB;
-      decode_tri(q, tA, tB);
-      const int i = P.pairs[2 * p], j = P.pairs[2 * p + 1];
+    while (true) {
+      if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7)) break;
+      const int qidx = item_q[islot];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(iempty0 + 8 * islot);
+      if (++islot == IQ) {
+        islot = 0;
+        iphase ^= 1;
+      }
+      if (qidx < 0) break;
+      const int4 it = P.items[qidx];
+      const FragDesc &F = P.frags[it.x];
+      const int i = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
       const bool same = (i == j), diag = (tA == tB);
+      const int nvpad = F.nvpad;
       if (!mbar_wait(tfull, (uint32_t)(nloc & 1), abort_flag, P.err, 4)) break;
       tc_fence_after();
       const int a = tA * TILE + row;
-      const float2 ea = P.ev2[a];
-      const float2 ei = P.eo2[i], ej = P.eo2[j];
+      const float2 ea = P.ev2[F.ev_off + a];
+      const float2 ei = P.eo2[F.eo_off + i], ej = P.eo2[F.eo_off + j];
       // e_i + e_j in hi/lo form (two-sum of the hi parts, lo parts added)
       const float sh = ei.x + ej.x;
       const float bv = sh - ei.x;
@@ -498,11 +592,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float dh0 = sh - ea.x;
       const float bw = dh0 - sh;
       const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
-      const float sa1 = P.inv_scale[i * nvpad + a];  // scale of column (a,i)
-      const float sa2 = P.inv_scale[j * nvpad + a];  // scale of column (a,j)
-      const float *sbj = P.inv_scale + j * nvpad + tB * TILE;
-      const float *sbi = P.inv_scale + i * nvpad + tB * TILE;
-      const float2 *evb = P.ev2 + tB * TILE;
+      const float *scl = P.inv_scale + F.col_base;
+      const float sa1 = scl[i * nvpad + a];  // scale of column (a,i)
+      const float sa2 = scl[j * nvpad + a];  // scale of column (a,j)
+      const float *sbj = scl + j * nvpad + tB * TILE;
+      const float *sbi = scl + i * nvpad + tB * TILE;
+      const float2 *evb = P.ev2 + F.ev_off + tB * TILE;
       const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
       const uint32_t t1 = tmem + lane_off;
       const uint32_t t2 = same ? t1 : t1 + 2 * TILE;
@@ -545,8 +640,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
       if (lane == 0) redd[ew] = eacc;
       asm volatile("bar.sync 1, 128;" ::: "memory");
-      if (ew == 0 && lane == 0) P.part[it] = (redd[0] + redd[1]) + (redd[2] + redd[3]);
+      if (ew == 0 && lane == 0) P.part[it.w] = (redd[0] + redd[1]) + (redd[2] + redd[3]);
       asm volatile("bar.sync 1, 128;" ::: "memory");
+      ++nloc;
     }
   }
   tc_fence_before();
@@ -554,6 +650,92 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+// --------------------------------------------------------------------------
+// reductions of a batch (deterministic, compensated)
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum_d(double a, double b, double &s, double &e) {
+  s = a + b;
+  const double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void warp_sum_comp_d(double &s, double &c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double s2 = __shfl_xor_sync(0xffffffffu, s, o);
+    const double c2 = __shfl_xor_sync(0xffffffffu, c, o);
+    double t, e;
+    if ((threadIdx.x & o) == 0)
+      two_sum_d(s, s2, t, e);
+    else
+      two_sum_d(s2, s, t, e);
+    s = t;
+    c = ((threadIdx.x & o) == 0 ? c + c2 : c2 + c) + e;
+  }
+}
+
+// one warp per (fragment, pair): Epair_f(i,j) = Epair_f(j,i) = sum of its items
+__global__ void pair_reduce_batch_kernel(const FragDesc *__restrict__ fr, int nfrag,
+                                         int npairs_total, const double *__restrict__ part) {
+  const int gp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gp >= npairs_total) return;
+  int lo = 0, hi = nfrag - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (fr[mid].pair_base <= gp)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const FragDesc &F = fr[lo];
+  const int p = gp - F.pair_base;
+  const double *src = part + F.item_base + (long long)p * F.ntp;
+  double s = 0.0, c = 0.0;
+  for (int r = lane; r < F.ntp; r += 32) {
+    double t, e;
+    two_sum_d(s, src[r], t, e);
+    s = t;
+    c += e;
+  }
+  warp_sum_comp_d(s, c);
+  if (lane == 0) {
+    int i, j;
+    decode_pair(p, i, j);
+    const double v = s + c;
+    F.Epair[i + (size_t)F.nocc * j] = v;
+    F.Epair[j + (size_t)F.nocc * i] = v;
+  }
+}
+
+// one block per fragment: Etot_f = sum_ij Epair_f(i,j)
+__global__ void total_reduce_batch_kernel(const FragDesc *__restrict__ fr) {
+  const FragDesc &F = fr[blockIdx.x];
+  __shared__ double ss[32], sc[32];
+  double s = 0.0, c = 0.0;
+  const size_t n = (size_t)F.nocc * F.nocc;
+  for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
+    double t, e;
+    two_sum_d(s, F.Epair[k], t, e);
+    s = t;
+    c += e;
+  }
+  warp_sum_comp_d(s, c);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    ss[w] = s;
+    sc[w] = c;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    s = lane < nw ? ss[lane] : 0.0;
+    c = lane < nw ? sc[lane] : 0.0;
+    warp_sum_comp_d(s, c);
+    if (lane == 0) *F.Etot = s + c;
   }
 }
 
@@ -575,116 +757,229 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 }
 
 int smem_bytes(int nsl, int nstage) {
-  return nstage * nsl * 2 * PANEL_BYTES + 1024 /*align*/ + 256 /*barriers etc*/;
+  return nstage * nsl * 2 * PANEL_BYTES + 1024 /*align*/ + 512 /*barriers, ring, etc*/;
 }
 
-template <int NSL, int NSTAGE>
-int launch_split(const CUtensorMap &tm, const SplitParams &P, int grid, cudaStream_t s) {
-  auto kern = split_energy_kernel<NSL, NSTAGE>;
-  const int smem = smem_bytes(NSL, NSTAGE);
-  RIMP2_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  kern<<<grid, NTHREADS, smem, s>>>(tm, P);
+// One slice-count group of a batch: its fragments share a slice count, a
+// slices buffer, one tensor map and one persistent launch.
+struct Group {
+  int nsl = 2;
+  int nfrag = 0;
+  std::vector<FragDesc> fh;
+  long long nitems = 0, R = 0, ncol_total = 0;
+  int npairs_total = 0, max_ncol = 0, max_nv = 0;
+  DevBuf frags, items, slices, inv, eo2, ev2, part, queue;
+  CUtensorMap tm;
+};
+
+int build_group(Group &g, cudaStream_t s) {
+  // heaviest fragments first: their items lead the queue
+  std::stable_sort(g.fh.begin(), g.fh.end(),
+                   [](const FragDesc &x, const FragDesc &y) { return x.nks > y.nks; });
+  long long row = 0, col = 0, item = 0;
+  int eo = 0, ev = 0, pb = 0;
+  for (auto &F : g.fh) {
+    F.nvpad = (F.nvirt + TILE - 1) / TILE * TILE;
+    F.nks = (F.NBA + KSTEP - 1) / KSTEP;
+    const int nt = F.nvpad / TILE;
+    F.ntp = nt * (nt + 1) / 2;
+    F.ncol = F.nocc * F.nvpad;
+    F.eo_off = eo;
+    F.ev_off = ev;
+    F.pair_base = pb;
+    F.row_base = row;
+    F.col_base = col;
+    F.item_base = item;
+    const int np = F.nocc * (F.nocc + 1) / 2;
+    eo += F.nocc;
+    ev += F.nvpad;
+    pb += np;
+    row += (long long)F.nks * F.ncol;
+    col += F.ncol;
+    item += (long long)np * F.ntp;
+    g.max_ncol = std::max(g.max_ncol, F.ncol);
+    g.max_nv = std::max(g.max_nv, std::max(F.nvpad, F.nocc));
+  }
+  g.nfrag = (int)g.fh.size();
+  g.nitems = item;
+  g.R = row;
+  g.ncol_total = col;
+  g.npairs_total = pb;
+  if (g.R > 2147483647LL - TILE || g.nitems > 2147483647LL) {
+    set_error("split batch too large for one launch (rows=%lld, items=%lld)", g.R, g.nitems);
+    return RIMP2_ERR_ARG;
+  }
+  RIMP2_TRY(g.frags.alloc(sizeof(FragDesc) * g.nfrag, s));
+  RIMP2_TRY(g.items.alloc(sizeof(int4) * (size_t)g.nitems, s));
+  RIMP2_TRY(g.slices.alloc(sizeof(__half) * (size_t)g.nsl * (size_t)g.R * 64, s));
+  RIMP2_TRY(g.inv.alloc(sizeof(float) * (size_t)g.ncol_total, s));
+  RIMP2_TRY(g.eo2.alloc(sizeof(float2) * (size_t)eo, s));
+  RIMP2_TRY(g.ev2.alloc(sizeof(float2) * (size_t)ev, s));
+  RIMP2_TRY(g.part.alloc(sizeof(double) * (size_t)g.nitems, s));
+  RIMP2_TRY(g.queue.alloc(sizeof(unsigned int), s));
+  RIMP2_CK(cudaMemcpyAsync(g.frags.p, g.fh.data(), sizeof(FragDesc) * g.nfrag,
+                           cudaMemcpyHostToDevice, s));
+  build_items_kernel<<<(unsigned)((g.nitems + 255) / 256), 256, 0, s>>>(
+      g.frags.as<FragDesc>(), g.nfrag, g.nitems, g.items.as<int4>());
   count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  auto encode = get_encode();
+  if (!encode) {
+    set_error("cuTensorMapEncodeTiled entry point unavailable");
+    return RIMP2_ERR_UNSUPPORTED;
+  }
+  cuuint64_t dims[3] = {64, (cuuint64_t)g.R, (cuuint64_t)g.nsl};
+  cuuint64_t strides[2] = {128, (cuuint64_t)g.R * 128};
+  cuuint32_t box[3] = {KSTEP, TILE, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult cr = encode(&g.tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, g.slices.p, dims, strides, box,
+                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+    return RIMP2_ERR_CUDA;
+  }
+  auto k2 = split_batch_kernel<2, 3>;
+  auto k3 = split_batch_kernel<3, 2>;
+  RIMP2_CK(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2, 3)));
+  RIMP2_CK(cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(3, 2)));
+  return RIMP2_OK;
+}
+
+// Enqueue one evaluation of the group on s (graph-capturable: no sync, no alloc).
+int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null */) {
+  if (g.nfrag == 0) return RIMP2_OK;
+  const FragDesc *fr = g.frags.as<FragDesc>();
+  if (ev) RIMP2_CK(cudaEventRecord(ev[0], s));
+  {
+    dim3 grid((unsigned)((g.max_ncol * 32LL + 255) / 256), (unsigned)g.nfrag);
+    slice_batch_kernel<<<grid, 256, 0, s>>>(fr, g.nsl, g.R * 64, g.slices.as<__half>(),
+                                            g.inv.as<float>());
+    dim3 g2((unsigned)((g.max_nv + 255) / 256), (unsigned)g.nfrag);
+    eps_batch_kernel<<<g2, 256, 0, s>>>(fr, g.eo2.as<float2>(), g.ev2.as<float2>());
+    count_launch(2);
+  }
+  RIMP2_CK(cudaMemsetAsync(g.queue.p, 0, sizeof(unsigned int), s));
+  BatchParams P;
+  P.frags = fr;
+  P.items = g.items.as<int4>();
+  P.nitems = g.nitems;
+  P.queue = g.queue.as<unsigned int>();
+  P.eo2 = g.eo2.as<float2>();
+  P.ev2 = g.ev2.as<float2>();
+  P.inv_scale = g.inv.as<float>();
+  P.part = g.part.as<double>();
+  P.err = device_error_word();
+  const int grid = (int)std::min<long long>(g.nitems, nsm);
+  if (inject_fault("launch")) {
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  if (ev) RIMP2_CK(cudaEventRecord(ev[1], s));
+  if (g.nsl == 2)
+    split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, P);
+  else
+    split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, P);
+  count_launch(1);
+  if (ev) RIMP2_CK(cudaEventRecord(ev[2], s));
+  pair_reduce_batch_kernel<<<(unsigned)((g.npairs_total + 7) / 8), 256, 0, s>>>(
+      fr, g.nfrag, g.npairs_total, g.part.as<double>());
+  total_reduce_batch_kernel<<<g.nfrag, 1024, 0, s>>>(fr);
+  count_launch(2);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;
 }
 
 }  // namespace
 
+// A planned batch: up to two slice-count groups, workspace and (optionally)
+// an instantiated CUDA graph of the whole evaluation.
+struct SplitPlan {
+  Group g[2];
+  int nsm = 0;
+  cudaGraphExec_t gexec = nullptr;
+  cudaGraph_t graph = nullptr;
+  ~SplitPlan() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
 bool split_supported() { return get_encode() != nullptr; }
 
-int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
-  (void)ms_kernel;
-  auto encode = get_encode();
-  if (!encode) {
-    set_error("cuTensorMapEncodeTiled entry point unavailable");
-    return RIMP2_ERR_UNSUPPORTED;
+int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nvirt, const int *NBA,
+                      const double *const *Ca, const double *const *eo, const double *const *ev,
+                      double *const *Epair, double *const *Etot, const int *nslices, bool graph,
+                      cudaStream_t s) {
+  *out = nullptr;
+  SplitPlan *P = new SplitPlan();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, dev);
+  P->g[0].nsl = 2;
+  P->g[1].nsl = 3;
+  for (int f = 0; f < nfrag; ++f) {
+    FragDesc F;
+    memset(&F, 0, sizeof F);
+    F.nocc = nocc[f];
+    F.nvirt = nvirt[f];
+    F.NBA = NBA[f];
+    F.Ca = Ca[f];
+    F.eo = eo[f];
+    F.ev = ev[f];
+    F.Epair = Epair[f];
+    F.Etot = Etot[f];
+    const int ns = nslices ? nslices[f] : 1;
+    P->g[ns >= 2 ? 1 : 0].fh.push_back(F);
   }
-  const int nsl = 1 + a.nslices;  // S0 + residual slices
-  const int nvpad = (a.nvirt + TILE - 1) / TILE * TILE;
-  const int Kpad = (a.NBA + KSTEP - 1) / KSTEP * KSTEP;
-  const int ntile = nvpad / TILE;
-  const int ntp = ntile * (ntile + 1) / 2;
-  const int npairs = a.nocc * (a.nocc + 1) / 2;
-  const long long ncol = (long long)nvpad * a.nocc;
-  const long long nitems = (long long)npairs * ntp;
-  if (ncol > (1LL << 31) - 1 || Kpad > (1 << 20)) {
-    set_error("split path: problem too large (ncol=%lld, Kpad=%d)", ncol, Kpad);
-    return RIMP2_ERR_ARG;
+  for (auto &g : P->g) {
+    if (g.fh.empty()) continue;
+    int rc = build_group(g, s);
+    if (rc != RIMP2_OK) {
+      delete P;
+      return rc;
+    }
   }
-  DevBuf slices, inv, eo2, ev2, pairs, part;
-  RIMP2_TRY(slices.alloc(sizeof(__half) * (size_t)nsl * ncol * Kpad, s));
-  RIMP2_TRY(inv.alloc(sizeof(float) * (size_t)ncol, s));
-  RIMP2_TRY(eo2.alloc(sizeof(float2) * (size_t)a.nocc, s));
-  RIMP2_TRY(ev2.alloc(sizeof(float2) * (size_t)nvpad, s));
-  RIMP2_TRY(pairs.alloc(sizeof(int) * 2 * (size_t)npairs, s));
-  RIMP2_TRY(part.alloc(sizeof(double) * (size_t)nitems, s));
+  if (graph) {
+    // the captured sequence needs the workspace already in place
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      set_error("graph capture start failed: %s", cudaGetErrorString(e));
+      delete P;
+      return RIMP2_ERR_CUDA;
+    }
+    int rc = RIMP2_OK;
+    for (auto &g : P->g)
+      if (rc == RIMP2_OK) rc = record_group(g, s, P->nsm, nullptr);
+    e = cudaStreamEndCapture(s, &P->graph);
+    if (rc != RIMP2_OK || e != cudaSuccess) {
+      if (rc == RIMP2_OK) set_error("graph capture failed: %s", cudaGetErrorString(e));
+      delete P;
+      return rc != RIMP2_OK ? rc : RIMP2_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&P->gexec, P->graph, 0);
+    if (e != cudaSuccess) {
+      set_error("graph instantiate failed: %s", cudaGetErrorString(e));
+      delete P;
+      return RIMP2_ERR_CUDA;
+    }
+  }
+  *out = P;
+  return RIMP2_OK;
+}
+
+int split_plan_execute(SplitPlan *P, cudaStream_t s) {
+  if (P->gexec) {
+    RIMP2_CK(cudaGraphLaunch(P->gexec, s));
+    count_launch(7);
+    return RIMP2_OK;
+  }
   const bool timed = timing_enabled();
   cudaEvent_t ev[4];
   if (timed)
     for (int k = 0; k < 4; ++k) RIMP2_CK(cudaEventCreate(&ev[k]));
-  if (timed) RIMP2_CK(cudaEventRecord(ev[0], s));
-  {
-    const long long thr = ncol * 32;
-    slice_kernel<<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(
-        a.Ca, a.NBA, a.nvirt, a.nocc, nvpad, Kpad, nsl, slices.as<__half>(), inv.as<float>());
-    const int n = (a.nocc > nvpad ? a.nocc : nvpad);
-    eps_split_kernel<<<(n + 255) / 256, 256, 0, s>>>(a.eo, a.nocc, a.ev, a.nvirt, nvpad,
-                                                     eo2.as<float2>(), ev2.as<float2>());
-    make_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(a.nocc, pairs.as<int>());
-    count_launch(3);
-    RIMP2_CK(cudaGetLastError());
-  }
-
-  CUtensorMap tm;
-  cuuint64_t dims[3] = {(cuuint64_t)Kpad, (cuuint64_t)ncol, (cuuint64_t)nsl};
-  cuuint64_t strides[2] = {(cuuint64_t)Kpad * 2, (cuuint64_t)Kpad * 2 * (cuuint64_t)ncol};
-  cuuint32_t box[3] = {KSTEP, TILE, 1};
-  cuuint32_t estr[3] = {1, 1, 1};
-  CUresult cr = encode(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, slices.p, dims, strides, box, estr,
-                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (cr != CUDA_SUCCESS) {
-    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
-    return RIMP2_ERR_CUDA;
-  }
-
-  int dev = 0, nsm = 0;
-  RIMP2_CK(cudaGetDevice(&dev));
-  RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  SplitParams P;
-  P.nocc = a.nocc;
-  P.nvpad = nvpad;
-  P.ntile = ntile;
-  P.ntp = ntp;
-  P.nks = Kpad / KSTEP;
-  P.nsl = nsl;
-  P.npairs = npairs;
-  P.nitems = nitems;
-  P.pairs = pairs.as<int>();
-  P.eo2 = eo2.as<float2>();
-  P.ev2 = ev2.as<float2>();
-  P.inv_scale = inv.as<float>();
-  P.part = part.as<double>();
-  P.err = device_error_word();
-  const int grid = (int)(nitems < nsm ? nitems : nsm);
-  if (inject_fault("launch")) {
-    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
-    return RIMP2_ERR_CUDA;
-  }
-  if (timed) RIMP2_CK(cudaEventRecord(ev[1], s));
-  if (nsl == 2)
-    RIMP2_TRY((launch_split<2, 3>(tm, P, grid, s)));
-  else
-    RIMP2_TRY((launch_split<3, 2>(tm, P, grid, s)));
-  if (timed) RIMP2_CK(cudaEventRecord(ev[2], s));
-
-  RIMP2_CK(cudaMemsetAsync(a.Epair, 0, sizeof(double) * (size_t)a.nocc * a.nocc, s));
-  pair_reduce_kernel<<<(npairs + 7) / 8, 256, 0, s>>>(part.as<double>(), ntp, pairs.as<int>(),
-                                                     npairs, a.nocc, a.Epair);
-  total_reduce_kernel<<<1, 1024, 0, s>>>(a.Epair, a.nocc, a.Etot);
-  count_launch(2);
-  RIMP2_CK(cudaGetLastError());
+  for (auto &g : P->g) RIMP2_TRY(record_group(g, s, P->nsm, timed ? ev : nullptr));
   if (timed) {
     RIMP2_CK(cudaEventRecord(ev[3], s));
     RIMP2_CK(cudaEventSynchronize(ev[3]));
@@ -696,6 +991,19 @@ int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
     for (int k = 0; k < 4; ++k) cudaEventDestroy(ev[k]);
   }
   return RIMP2_OK;
+}
+
+void split_plan_destroy(SplitPlan *P) { delete P; }
+
+int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
+  (void)ms_kernel;
+  SplitPlan *P = nullptr;
+  const int ns = a.nslices;
+  RIMP2_TRY(split_plan_create(&P, 1, &a.nocc, &a.nvirt, &a.NBA, &a.Ca, &a.eo, &a.ev, &a.Epair,
+                              &a.Etot, &ns, false, s));
+  int rc = split_plan_execute(P, s);
+  split_plan_destroy(P);  // workspace is released stream-ordered
+  return rc;
 }
 
 }  // namespace rimp2
