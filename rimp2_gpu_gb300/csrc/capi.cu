@@ -697,9 +697,11 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
 // Residual slices per element by shape bucket, chosen so that the pair and
 // total energies stay within 1e-7 relative of FP64: one residual slice
 // suffices once the pair sums average over enough (a,b) terms, small
-// fragments get two.  Buckets are keyed by nvirt (the (a,b) count per pair);
-// the autotuner (rimp2_gpu_gb300/autotune.py) may replace the table.
-static std::vector<std::pair<int, int>> g_buckets = {{0, 2}, {256, 1}};
+// fragments get two.  Buckets are keyed by nvirt (the (a,b) count per pair).
+// Default = the table measured by rimp2_gpu_gb300/autotune.py on GB300 with a
+// 2x margin on the 1e-7 target (rimp2_gpu_gb300/tuning/split_buckets.json);
+// rimp2_set_split_buckets replaces it.
+static std::vector<std::pair<int, int>> g_buckets = {{0, 2}, {384, 1}};
 static std::mutex g_bucket_mu;
 
 int rimp2_split_nslices(int nvirt, int nocc, int NBA) {

@@ -74,5 +74,7 @@ def test_bucket_table_roundtrip():
     from rimp2_gpu_gb300 import api
     api.set_split_buckets([0, 128], [2, 1])
     assert api.split_nslices(100, 4, 64) == 2 and api.split_nslices(200, 4, 64) == 1
-    api.set_split_buckets([0, 256], [2, 1])  # library default
-    assert api.split_nslices(200, 4, 64) == 2
+    from rimp2_gpu_gb300 import autotune
+    import os
+    t = autotune.load(os.path.join(os.path.dirname(api.__file__), "tuning", "split_buckets.json"))
+    assert api.split_nslices(200, 4, 64) == 2 and t["buckets"][0]["nvirt_min"] == 0

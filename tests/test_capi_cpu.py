@@ -72,3 +72,14 @@ def test_product_does_not_import_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".F90")):
                 txt = open(os.path.join(dp, f)).read()
                 assert "oracle" not in txt.replace("the oracle is", ""), f
+
+
+def test_default_buckets_match_committed_tuning_table():
+    import json
+    from rimp2_gpu_gb300 import api
+    t = json.load(open(os.path.join(ROOT, "rimp2_gpu_gb300", "tuning", "split_buckets.json")))
+    for b in t["buckets"]:
+        for nv in (b["nvirt_min"], b["nvirt_min"] + 1):
+            assert api.split_nslices(max(nv, 1), 8, 256) == b["nslices"] or any(
+                c["nvirt_min"] <= nv and c["nvirt_min"] > b["nvirt_min"] for c in t["buckets"])
+        assert b["worst_rel_err"][str(b["nslices"])] <= t["target"] * t["margin"]
