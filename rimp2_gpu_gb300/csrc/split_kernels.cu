@@ -53,7 +53,7 @@ namespace {
 constexpr int TILE = 128;      // a/b tile edge (MMA M and N)
 constexpr int KSTEP = 64;      // K per stage (one 128-byte swizzle row of FP16)
 constexpr int PANEL_BYTES = TILE * KSTEP * 2;  // 16 KB
-constexpr int NTHREADS = 192;
+constexpr int NTHREADS = 320;  // producer warp, MMA warp, 8 epilogue warps
 constexpr long long WAIT_BUDGET = 4000000000LL;  // ~2 s of SM clock per wait
 
 // --------------------------------------------------------------------------
@@ -385,34 +385,41 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int STAGE_BYTES = NSL * 2 * PANEL_BYTES;
+  constexpr int NEPI = 8;  // epilogue warps: two per TMEM lane quadrant
   uint8_t *stages = base;
   uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
-  // bars: full[NSTAGE], empty[NSTAGE], tmem_full, tmem_empty, drain, item_full[IQ], item_empty[IQ]
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NSTAGE + 3 + 2 * IQ);
+  // bars: full[NSTAGE], empty[NSTAGE], t1full, t1empty, t2full, t2empty, drain,
+  //       item_full[IQ], item_empty[IQ]
+  constexpr int NB = 2 * NSTAGE + 5 + 2 * IQ;
+  uint32_t *tmem_slot = (uint32_t *)(bars + NB);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   volatile int *item_q = (volatile int *)(tmem_slot + 2);  // [IQ]
-  double *redd = (double *)(((uintptr_t)(tmem_slot + 2 + IQ) + 7) & ~(uintptr_t)7);  // [4]
+  double *redd = (double *)(((uintptr_t)(tmem_slot + 2 + IQ) + 7) & ~(uintptr_t)7);  // [NEPI]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(&bars[0]);
   const uint32_t empty0 = smem_u32(&bars[NSTAGE]);
-  const uint32_t tfull = smem_u32(&bars[2 * NSTAGE]);
-  const uint32_t tempty = smem_u32(&bars[2 * NSTAGE + 1]);
-  const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 2]);
-  const uint32_t ifull0 = smem_u32(&bars[2 * NSTAGE + 3]);
-  const uint32_t iempty0 = smem_u32(&bars[2 * NSTAGE + 3 + IQ]);
+  const uint32_t t1full = smem_u32(&bars[2 * NSTAGE]);
+  const uint32_t t1empty = smem_u32(&bars[2 * NSTAGE + 1]);
+  const uint32_t t2full = smem_u32(&bars[2 * NSTAGE + 2]);
+  const uint32_t t2empty = smem_u32(&bars[2 * NSTAGE + 3]);
+  const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 4]);
+  const uint32_t ifull0 = smem_u32(&bars[2 * NSTAGE + 5]);
+  const uint32_t iempty0 = smem_u32(&bars[2 * NSTAGE + 5 + IQ]);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
     }
-    mbar_init(tfull, 1);
-    mbar_init(tempty, 4);
+    mbar_init(t1full, 1);
+    mbar_init(t1empty, NEPI);
+    mbar_init(t2full, 1);
+    mbar_init(t2empty, NEPI);
     mbar_init(drain, 1);
     for (int s = 0; s < IQ; ++s) {
       mbar_init(ifull0 + 8 * s, 1);
-      mbar_init(iempty0 + 8 * s, 5);  // MMA issuer + 4 epilogue warps
+      mbar_init(iempty0 + 8 * s, 1 + NEPI);  // MMA issuer + epilogue warps
     }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -506,14 +513,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int nks = P.frags[it.x].nks;
         const int i = it.y & 0xFFFF, j = it.y >> 16;
         const int ntiles = (i == j) ? 1 : 2;
-        if (nloc > 0) {  // epilogue must have drained TMEM of the previous item
-          if (!mbar_wait(tempty, (uint32_t)((nloc - 1) & 1), abort_flag, P.err, 2)) break;
-        }
-        tc_fence_after();
-        for (int t = 0; t < ntiles && ok; ++t) {
+        for (int t = 0; t < 2 && ok; ++t) {
+          // tile t's accumulators must have been read out for the previous item
+          if (nloc > 0 &&
+              !mbar_wait(t == 0 ? t1empty : t2empty, (uint32_t)((nloc - 1) & 1), abort_flag, P.err,
+                         2)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
           const uint32_t dL0 = tmem + (uint32_t)(t * 2 * TILE);
           const uint32_t dL1 = dL0 + TILE;
-          for (int kc = 0; kc < nks; ++kc) {
+          for (int kc = 0; t < ntiles && kc < nks; ++kc) {
             if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err, 3)) {
               ok = false;
               break;
@@ -545,9 +556,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               phase ^= 1;
             }
           }
+          if (!ok) break;
+          mma_commit(t == 0 ? t1full : t2full);  // tile t of this item is complete
         }
         if (!ok) break;
-        mma_commit(tfull);  // accumulators of this item complete
         ++nloc;
       }
       // drain: all MMAs issued by this thread complete before TMEM is freed
@@ -558,9 +570,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else {
     // ------------------------------ epilogue ----------------------------------
-    const int ew = warp - 2;           // 0..3
-    const int quad = warp & 3;         // TMEM lane quadrant this warp may access
-    const int row = quad * 32 + lane;  // tile row = a offset
+    const int ew = warp - 2;             // 0..7
+    const int quad = warp & 3;           // TMEM lane quadrant this warp may access
+    const int cbase = (ew >> 2) * 64;    // column half of the tile this warp reads
+    const int row = quad * 32 + lane;    // tile row = a offset
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     int islot = 0;
     uint32_t iphase = 0;
     long long nloc = 0;
@@ -579,9 +593,31 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int i = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
       const bool same = (i == j), diag = (tA == tB);
       const int nvpad = F.nvpad;
-      if (!mbar_wait(tfull, (uint32_t)(nloc & 1), abort_flag, P.err, 4)) break;
-      tc_fence_after();
       const int a = tA * TILE + row;
+      const float *scl = P.inv_scale + F.col_base;
+      const float sa1 = scl[i * nvpad + a];  // scale of column (a,i)
+      const float sa2 = scl[j * nvpad + a];  // scale of column (a,j)
+      const float *sbj = scl + j * nvpad + tB * TILE + cbase;
+      const float *sbi = scl + i * nvpad + tB * TILE + cbase;
+      const float2 *evb = P.ev2 + F.ev_off + tB * TILE + cbase;
+      // ---- T1 -> registers, then hand its TMEM back to the MMA issuer ----
+      if (!mbar_wait(t1full, (uint32_t)(nloc & 1), abort_flag, P.err, 4)) break;
+      tc_fence_after();
+      const uint32_t t1 = tmem + lane_off + cbase;
+      float g1[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16) {
+        float l0[16], l1[16];
+        tmem_ld16(t1 + c0, l0);
+        tmem_ld16(t1 + TILE + c0, l1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g1[c0 + k] = (l0[k] + l1[k]) * (sa1 * sbj[c0 + k]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(t1empty);
+      // ---- denominators ----
       const float2 ea = P.ev2[F.ev_off + a];
       const float2 ei = P.eo2[F.eo_off + i], ej = P.eo2[F.eo_off + j];
       // e_i + e_j in hi/lo form (two-sum of the hi parts, lo parts added)
@@ -592,56 +628,55 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float dh0 = sh - ea.x;
       const float bw = dh0 - sh;
       const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
-      const float *scl = P.inv_scale + F.col_base;
-      const float sa1 = scl[i * nvpad + a];  // scale of column (a,i)
-      const float sa2 = scl[j * nvpad + a];  // scale of column (a,j)
-      const float *sbj = scl + j * nvpad + tB * TILE;
-      const float *sbi = scl + i * nvpad + tB * TILE;
-      const float2 *evb = P.ev2 + F.ev_off + tB * TILE;
-      const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
-      const uint32_t t1 = tmem + lane_off;
-      const uint32_t t2 = same ? t1 : t1 + 2 * TILE;
+      // ---- T2 and the energy terms ----
+      if (!mbar_wait(t2full, (uint32_t)(nloc & 1), abort_flag, P.err, 8)) break;
+      tc_fence_after();
+      const uint32_t t2 = tmem + lane_off + 2 * TILE + cbase;
       double eacc = 0.0;
-#pragma unroll 1
-      for (int c0 = 0; c0 < TILE; c0 += 16) {
-        float l01[16], l11[16], l02[16], l12[16];
-        tmem_ld16(t1 + c0, l01);
-        tmem_ld16(t1 + TILE + c0, l11);
-        tmem_ld16(t2 + c0, l02);
-        tmem_ld16(t2 + TILE + c0, l12);
-        tmem_wait_ld();
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16) {
+        float g2[16];
+        if (same) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) g2[k] = g1[c0 + k];
+        } else {
+          float l0[16], l1[16];
+          tmem_ld16(t2 + c0, l0);
+          tmem_ld16(t2 + TILE + c0, l1);
+          tmem_wait_ld();
+#pragma unroll
+          for (int k = 0; k < 16; ++k) g2[k] = (l0[k] + l1[k]) * (sa2 * sbi[c0 + k]);
+        }
         float ef = 0.0f;
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-          const int b = c0 + k;
-          const float2 eb = evb[b];
-          const float g1 = (l01[k] + l11[k]) * (sa1 * sbj[b]);
-          const float g2 = (l02[k] + l12[k]) * (sa2 * sbi[b]);
+          const float2 eb = evb[c0 + k];
+          const float x1 = g1[c0 + k], x2 = g2[k];
           // d = (dh0 + dl0) - (eb.x + eb.y) with the leading subtraction exact
           const float dh = dh0 - eb.x;
           const float bz = dh - dh0;
           const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
           const float r = __frcp_rn(d);
-          float num;
-          if (diag) {
-            num = g1 * fmaf(2.0f, g1, -g2);
-          } else {
-            num = 2.0f * fmaf(g1, g1 - g2, g2 * g2);
-          }
+          const float num = diag ? x1 * fmaf(2.0f, x1, -x2) : 2.0f * fmaf(x1, x1 - x2, x2 * x2);
           ef = fmaf(num, r, ef);
         }
         eacc += (double)ef;
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(tempty);
-      // reduce the item's energy over the 128 epilogue threads
+      if (lane == 0) mbar_arrive(t2empty);
+      // reduce the item's energy over the epilogue threads
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
       if (lane == 0) redd[ew] = eacc;
-      asm volatile("bar.sync 1, 128;" ::: "memory");
-      if (ew == 0 && lane == 0) P.part[it.w] = (redd[0] + redd[1]) + (redd[2] + redd[3]);
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (ew == 0 && lane == 0) {
+        double tot = 0.0;
+#pragma unroll
+        for (int w = 0; w < NEPI; ++w) tot += redd[w];
+        P.part[it.w] = tot;
+      }
+      asm volatile("bar.sync 1, 256;" ::: "memory");
       ++nloc;
     }
   }
