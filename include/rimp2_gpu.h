@@ -221,6 +221,20 @@ int rimp2_gen_fragment_dev(unsigned long long seed, int nocc, int nvirt, int NBA
  * Cmo(nbas,nbas) columns occ then virt; Calpha out (NBA,nvirt,nocc). */
 int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc, const int *nvirt,
                          const double *ao, const double *V, const double *Cmo, double *Calpha);
+/* Device-pointer form on `stream` (synchronises once: the metric's
+ * positive-definiteness is checked before the solve). */
+int rimp2_calpha_from_ao_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao,
+                             const double *dV, const double *dCmo, double *dCalpha, void *stream);
+/* Building blocks: lower Cholesky V = L L^T in place (n x n, strict upper
+ * zeroed; RIMP2_ERR_ARG if not positive definite) and X = L^{-1} B
+ * (B n x m, overwritten as workspace; X separate). FP64, blocked, GPU. */
+int rimp2_cholesky_dev(int n, double *dV, void *stream);
+int rimp2_trsm_lower_dev(int n, int m, const double *dL, double *dB, double *dX, void *stream);
+/* Synthetic AO inputs on the device: (alpha|mu nu) = N(0,1) exp(-|mu-nu|/32),
+ * symmetric in (mu,nu); V = A A^T/NBA + 0.1 I with A ~ N(0,1).  Either
+ * output may be NULL. */
+int rimp2_gen_ao_dev(unsigned long long seed, int NBA, int nbas, double *dao, double *dV,
+                     void *stream);
 
 #ifdef __cplusplus
 }

@@ -246,6 +246,23 @@ def calpha_from_ao(NBA, nbas, nocc, nvirt, ao, V, Cmo):
     return out
 
 
+def calpha_from_ao_dev(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, stream=0):
+    call("rimp2_calpha_from_ao_dev", NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha,
+         stream or None)
+
+
+def cholesky_dev(n, dV, stream=0):
+    call("rimp2_cholesky_dev", n, dV, stream or None)
+
+
+def trsm_lower_dev(n, m, dL, dB, dX, stream=0):
+    call("rimp2_trsm_lower_dev", n, m, dL, dB, dX, stream or None)
+
+
+def gen_ao_dev(seed, NBA, nbas, dao=0, dV=0, stream=0):
+    call("rimp2_gen_ao_dev", seed, NBA, nbas, dao or None, dV or None, stream or None)
+
+
 def get_dev_mem():
     """(total, free) device memory in bytes (replaces get_dev_mem, cuda_api.cu:5-8)."""
     t = C.c_size_t()

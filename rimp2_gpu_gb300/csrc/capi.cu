@@ -910,19 +910,4 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
   return finish(s);
 }
 
-int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc, const int *nvirt,
-                         const double *ao, const double *V, const double *Cmo, double *Calpha) {
-  clear_error();
-  (void)NBA;
-  (void)nbas;
-  (void)nocc;
-  (void)nvirt;
-  (void)ao;
-  (void)V;
-  (void)Cmo;
-  (void)Calpha;
-  set_error("rimp2_calpha_from_ao: not built yet");
-  return RIMP2_ERR_UNSUPPORTED;
-}
-
 }  // extern "C"

@@ -1,0 +1,82 @@
+"""AO front end on the GPU (FP64): AO->MO transform, metric Cholesky and the
+triangular solve that forms Calpha, against the CPU oracle (1e-10 relative
+to the largest element), and the energy built on it."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def t(a):
+    import torch
+    return torch.from_numpy(np.asfortranarray(a).ravel(order="F")).cuda()
+
+
+def close(x, ref, rel):
+    err = np.abs(x - ref).max() / np.abs(ref).max()
+    assert err <= rel, err
+
+
+@pytest.mark.parametrize("NBA,nbas,nocc", [(96, 40, 4), (130, 50, 5), (64, 24, 3)])
+def test_calpha_from_ao_vs_oracle(NBA, nbas, nocc):
+    from rimp2_gpu_gb300 import api
+    nvirt = nbas - nocc
+    ao = O.gen_ao3c(3, NBA, nbas)
+    V = O.gen_metric(3, NBA)
+    Cm = O.gen_mo(3, nbas)
+    B = O.ao2mo(NBA, nbas, nocc, nvirt, ao, Cm)
+    L = O.cholesky(V)
+    ref = O.trsm_lower(L, B.reshape(NBA, -1, order="F")).reshape(B.shape, order="F")
+    got = api.calpha_from_ao(NBA, nbas, nocc, nvirt, ao, V, Cm)
+    close(got, ref, 1e-10)
+    # energy on top of it (split path) within the energy bar of FP64
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, ref, np.sort(np.linspace(-1.2, -0.4, nocc)),
+                              np.sort(np.linspace(0.2, 2.5, nvirt)))
+    Ep, E = api.energy(nvirt, nocc, NBA, np.asfortranarray(got), np.sort(np.linspace(-1.2, -0.4, nocc)),
+                       np.sort(np.linspace(0.2, 2.5, nvirt)), precision=api.PREC_SPLIT)
+    assert abs(E - Er) <= 1e-7 * abs(Er)
+
+
+def test_device_ao_generators_match_oracle():
+    import torch
+    from rimp2_gpu_gb300 import api
+    NBA, nbas = 70, 33
+    dao = torch.zeros(NBA * nbas * nbas, dtype=torch.float64, device="cuda")
+    dV = torch.zeros(NBA * NBA, dtype=torch.float64, device="cuda")
+    api.gen_ao_dev(5, NBA, nbas, dao.data_ptr(), dV.data_ptr())
+    torch.cuda.synchronize()
+    close(dao.cpu().numpy(), O.gen_ao3c(5, NBA, nbas).ravel(order="F"), 1e-14)
+    close(dV.cpu().numpy(), O.gen_metric(5, NBA).ravel(order="F"), 1e-13)
+
+
+def test_cholesky_and_solve_blocks():
+    import torch
+    from rimp2_gpu_gb300 import api
+    n, m = 200, 37  # several 64-blocks plus a ragged one
+    V = O.gen_metric(8, n)
+    dV = t(V)
+    api.cholesky_dev(n, dV.data_ptr())
+    torch.cuda.synchronize()
+    L = dV.cpu().numpy().reshape(n, n, order="F")
+    close(L, O.cholesky(V), 1e-12)
+    assert np.all(np.triu(L, 1) == 0)
+    Bm = O.gen_matrix(8, 9, n, m)
+    dB, dX = t(Bm), torch.zeros(n * m, dtype=torch.float64, device="cuda")
+    api.trsm_lower_dev(n, m, dV.data_ptr(), dB.data_ptr(), dX.data_ptr())
+    torch.cuda.synchronize()
+    close(dX.cpu().numpy().reshape(n, m, order="F"), O.trsm_lower(L, Bm), 1e-11)
+
+
+def test_cholesky_rejects_indefinite_metric():
+    import torch
+    from rimp2_gpu_gb300 import api, _lib
+    n = 70
+    V = O.gen_metric(8, n)
+    V[65, 65] = -5.0  # a negative pivot in the second block
+    dV = t(V)
+    with pytest.raises(_lib.Rimp2Error) as ei:
+        api.cholesky_dev(n, dV.data_ptr())
+    assert ei.value.status == 1 and "positive definite" in str(ei.value)
+    torch.cuda.synchronize()
