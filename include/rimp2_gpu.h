@@ -55,6 +55,11 @@ long long rimp2_kernel_launch_count(void);
  * kernel): RIMP2_ERR_TIMEOUT, else RIMP2_OK.  Host-pointer entry points do
  * this themselves before returning. */
 int rimp2_sync_status(void *stream);
+/* Failure-detection self-test: a one-thread kernel waits on an mbarrier that
+ * nothing completes, with the production kernels' bounded-wait code and a
+ * budget of budget_cycles SM clocks (<= 1e9).  Expected result:
+ * RIMP2_ERR_TIMEOUT, with the library usable afterwards. */
+int rimp2_selftest_bounded_wait(long long budget_cycles, void *stream);
 /* Opt-in CUDA-event timing of the split path's phases; rimp2_last_timing
  * fills ms4 = {slicing, energy kernel, reductions, 0} of the last call. */
 int rimp2_set_timing(int on);

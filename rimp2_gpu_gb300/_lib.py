@@ -29,6 +29,7 @@ SIGNATURES = {
     "rimp2_kernel_launch_count": ([], C.c_longlong),
     "rimp2_sync_status": ([_vp], C.c_int),
     "rimp2_set_timing": ([C.c_int], C.c_int),
+    "rimp2_selftest_bounded_wait": ([C.c_longlong, _vp], C.c_int),
     "rimp2_last_timing": ([C.POINTER(C.c_float)], C.c_int),
     "rimp2_probe_fp64_peak": ([_dp], C.c_int),
     "rimp2_calc_tocca": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp], C.c_int),

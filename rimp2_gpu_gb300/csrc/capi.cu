@@ -373,6 +373,15 @@ int rimp2_sync_status(void *stream) {
   return collect_device_error(s);
 }
 
+int rimp2_selftest_bounded_wait(long long budget_cycles, void *stream) {
+  clear_error();
+  RIMP2_REQ(budget_cycles > 0 && budget_cycles <= 1000000000LL,
+            "rimp2_selftest_bounded_wait: budget must be in (0, 1e9] cycles");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  return bounded_wait_selftest(budget_cycles, s);
+}
+
 int rimp2_set_timing(int on) {
   g_timing = (on != 0);
   return RIMP2_OK;

@@ -120,6 +120,7 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
                       cudaStream_t s);
 int split_plan_execute(SplitPlan *P, cudaStream_t s);
 void split_plan_destroy(SplitPlan *P);
+int bounded_wait_selftest(long long budget_cycles, cudaStream_t s);
 bool split_supported();
 
 }  // namespace rimp2

@@ -92,11 +92,11 @@ __device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
 // error word) if the phase does not complete within the clock budget or if
 // another role already aborted.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
-                                          int *err, int code) {
+                                          int *err, int code, long long budget = WAIT_BUDGET) {
   const long long t0 = clock64();
   while (!mbar_test(bar, parity)) {
     if (*abort_flag) return false;
-    if (clock64() - t0 > WAIT_BUDGET) {
+    if (clock64() - t0 > budget) {
       *abort_flag = 1;
       atomicCAS(err, 0, code);
       return false;
@@ -688,6 +688,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   }
 }
 
+// Self-test of the bounded-wait path: one thread waits on an mbarrier that
+// nothing ever completes, with a short clock budget.  The wait must give up,
+// raise the CTA abort flag and record `code` in the device error word, and
+// the kernel must return normally.
+__global__ void wait_selftest_kernel(long long budget, int *err) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar), 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const bool ok = mbar_wait(smem_u32(&bar), 0, (volatile int *)&abort_flag, err, 99, budget);
+    if (ok) atomicCAS(err, 0, 98);  // cannot happen: nothing arrives
+  }
+  __syncthreads();
+}
+
 // --------------------------------------------------------------------------
 // reductions of a batch (deterministic, compensated)
 // --------------------------------------------------------------------------
@@ -1029,6 +1049,13 @@ int split_plan_execute(SplitPlan *P, cudaStream_t s) {
 }
 
 void split_plan_destroy(SplitPlan *P) { delete P; }
+
+int bounded_wait_selftest(long long budget_cycles, cudaStream_t s) {
+  wait_selftest_kernel<<<1, 32, 0, s>>>(budget_cycles, device_error_word());
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return collect_device_error(s);
+}
 
 int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
   (void)ms_kernel;

@@ -168,3 +168,27 @@ def test_fault_injection_alloc(api, monkeypatch):
     monkeypatch.delenv("RIMP2_FAULT_INJECT")
     Ep, E = api.energy(8, 2, 8, Ca, eo, ev)  # the library stays usable
     assert np.isfinite(E)
+
+
+def test_fault_injection_launch(api, monkeypatch):
+    from rimp2_gpu_gb300 import _lib
+    Ca, eo, ev = O.gen_fragment(3, 2, 8, 8)
+    monkeypatch.setenv("RIMP2_FAULT_INJECT", "launch")
+    with pytest.raises(_lib.Rimp2Error) as ei:
+        api.energy(8, 2, 8, Ca, eo, ev, precision=api.PREC_SPLIT)
+    assert ei.value.status == 2 and "injected" in str(ei.value)
+    monkeypatch.delenv("RIMP2_FAULT_INJECT")
+    Ep, E = api.energy(8, 2, 8, Ca, eo, ev, precision=api.PREC_SPLIT)
+    assert np.isfinite(E)
+
+
+def test_bounded_wait_gives_up_and_library_recovers(api):
+    """A device wait on a barrier nothing completes must end by its clock
+    budget with RIMP2_ERR_TIMEOUT (no hang, no trap), and the next call works."""
+    st = api.lib().rimp2_selftest_bounded_wait(2_000_000, None)  # ~1 ms of SM clock
+    assert st == 5, api.last_error()
+    assert "bounded wait" in api.last_error()
+    Ca, eo, ev = O.gen_fragment(4, 3, 40, 50)
+    Epr, Er = O.pair_energies(40, 3, 50, Ca, eo, ev)
+    Ep, E = api.energy(40, 3, 50, Ca, eo, ev, precision=api.PREC_SPLIT)
+    assert abs(E - Er) <= 1e-7 * abs(Er)
