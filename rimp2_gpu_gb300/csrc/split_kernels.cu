@@ -378,6 +378,7 @@ struct BatchParams {
 };
 
 constexpr int IQ = 4;  // item ring depth between the producer and the consumers
+constexpr int TP = TILE + 1;  // padded row of the diagonal-tile transpose buffer (floats)
 
 template <int NSL, int NSTAGE>
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -395,6 +396,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   volatile int *item_q = (volatile int *)(tmem_slot + 2);  // [IQ]
   double *redd = (double *)(((uintptr_t)(tmem_slot + 2 + IQ) + 7) & ~(uintptr_t)7);  // [NEPI]
+  // transpose buffer for diagonal tile pairs: 64 rows of T1, padded rows
+  float *tbuf = (float *)(base + NSTAGE * STAGE_BYTES + 512);  // [64][TP]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(&bars[0]);
@@ -458,7 +461,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int4 it = P.items[qidx];
         const FragDesc &F = P.frags[it.x];
         const int i = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
-        const int ntiles = (i == j) ? 1 : 2;
+        // T2 = T1 for i == j, and T2 = T1^T (shared-memory transpose) for A == B
+        const int ntiles = (i == j || tA == tB) ? 1 : 2;
         for (int t = 0; t < ntiles && ok; ++t) {
           const int colA = (t == 0 ? i : j) * F.nvpad + tA * TILE;
           const int colB = (t == 0 ? j : i) * F.nvpad + tB * TILE;
@@ -511,8 +515,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (qidx < 0) break;
         const int4 it = P.items[qidx];
         const int nks = P.frags[it.x].nks;
-        const int i = it.y & 0xFFFF, j = it.y >> 16;
-        const int ntiles = (i == j) ? 1 : 2;
+        const int i = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
+        const int ntiles = (i == j || tA == tB) ? 1 : 2;
         for (int t = 0; t < 2 && ok; ++t) {
           // tile t's accumulators must have been read out for the previous item
           if (nloc > 0 &&
@@ -632,21 +636,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!mbar_wait(t2full, (uint32_t)(nloc & 1), abort_flag, P.err, 8)) break;
       tc_fence_after();
       const uint32_t t2 = tmem + lane_off + 2 * TILE + cbase;
-      double eacc = 0.0;
-#pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16) {
-        float g2[16];
-        if (same) {
-#pragma unroll
-          for (int k = 0; k < 16; ++k) g2[k] = g1[c0 + k];
-        } else {
-          float l0[16], l1[16];
-          tmem_ld16(t2 + c0, l0);
-          tmem_ld16(t2 + TILE + c0, l1);
-          tmem_wait_ld();
-#pragma unroll
-          for (int k = 0; k < 16; ++k) g2[k] = (l0[k] + l1[k]) * (sa2 * sbi[c0 + k]);
-        }
+      // one 16-column chunk of energy terms, g2 supplied by `g2at(k)`
+      auto terms = [&](int c0, const float *g2) -> float {
         float ef = 0.0f;
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
@@ -660,7 +651,48 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const float num = diag ? x1 * fmaf(2.0f, x1, -x2) : 2.0f * fmaf(x1, x1 - x2, x2 * x2);
           ef = fmaf(num, r, ef);
         }
-        eacc += (double)ef;
+        return ef;
+      };
+      double eacc = 0.0;
+      if (diag && !same) {
+        // T2[a,b] = g_ij(b,a) = T1[b,a]: transpose T1 through shared memory in
+        // two 64-row passes; pass h serves the warps that own columns [64h,64h+64)
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+          asm volatile("bar.sync 1, 256;" ::: "memory");
+          if ((row >> 6) == h) {
+            float *dst = tbuf + (row - 64 * h) * TP + cbase;
+#pragma unroll
+            for (int k = 0; k < 64; ++k) dst[k] = g1[k];
+          }
+          asm volatile("bar.sync 1, 256;" ::: "memory");
+          if ((cbase >> 6) == h) {
+#pragma unroll
+            for (int c0 = 0; c0 < 64; c0 += 16) {
+              float g2[16];
+#pragma unroll
+              for (int k = 0; k < 16; ++k) g2[k] = tbuf[(c0 + k) * TP + row];
+              eacc += (double)terms(c0, g2);
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+          float g2[16];
+          if (same) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) g2[k] = g1[c0 + k];
+          } else {
+            float l0[16], l1[16];
+            tmem_ld16(t2 + c0, l0);
+            tmem_ld16(t2 + TILE + c0, l1);
+            tmem_wait_ld();
+#pragma unroll
+            for (int k = 0; k < 16; ++k) g2[k] = (l0[k] + l1[k]) * (sa2 * sbi[c0 + k]);
+          }
+          eacc += (double)terms(c0, g2);
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -812,7 +844,8 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 }
 
 int smem_bytes(int nsl, int nstage) {
-  return nstage * nsl * 2 * PANEL_BYTES + 1024 /*align*/ + 512 /*barriers, ring, etc*/;
+  return nstage * nsl * 2 * PANEL_BYTES + 1024 /*align*/ + 512 /*barriers, ring, etc*/ +
+         64 * TP * 4 /*diagonal-tile transpose buffer*/;
 }
 
 // One slice-count group of a batch: its fragments share a slice count, a
