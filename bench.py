@@ -151,7 +151,7 @@ def measured_peaks():
 def traffic_per_launch():
     """DRAM bytes per launch of the energy kernel from the committed ncu
     capture summary (scaled to this workload), or None."""
-    p = os.path.join(ROOT, "profiles", "split_energy_kernel_traffic.json")
+    p = os.path.join(ROOT, "profiles", "split_batch_kernel_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
@@ -397,7 +397,7 @@ def run_ours(args):
     roof = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",
             "frac": achieved / burst, "traffic": traffic_per_launch(),
             "peak_source": f"{src} bf16_tflops (burst); fp16 kind::f16 runs at the bf16 rate",
-            "kernel": "split_energy_kernel", "kernel_ms": kmed,
+            "kernel": "split_batch_kernel", "kernel_ms": kmed,
             "performed_tflops": performed / (kmed * 1e-3) / 1e12,
             "performed_frac": performed / (kmed * 1e-3) / 1e12 / burst,
             "performed_frac_of_sustained": performed / (kmed * 1e-3) / 1e12 / sustained,
