@@ -24,11 +24,18 @@ from . import api
 
 TARGET = 1e-7
 BUCKET_EDGES = [64, 128, 192, 256, 384]          # nvirt_min of each bucket
-SAMPLE = {64: [(8, 64, 256), (24, 96, 1024)],
-          128: [(16, 128, 512), (8, 160, 2048)],
-          192: [(12, 192, 384), (24, 224, 1024)],
-          256: [(8, 256, 256), (16, 320, 2048)],
-          384: [(8, 384, 512), (16, 512, 1024)]}
+BUCKET_TOP = [128, 192, 256, 384, 513]
+
+
+def _sample(lo, hi):
+    """Fragments at the bucket's low edge (fewest (a,b) terms per pair: the
+    worst case for averaging), middle and top, with few and many occupied
+    orbitals and short and long auxiliary spaces."""
+    nv = [lo, lo + 1, (lo + hi) // 2, hi - 1]
+    return [(o, v, b) for v in nv for (o, b) in ((8, 256), (40, 512), (16, 2048))]
+
+
+SAMPLE = {lo: _sample(lo, hi) for lo, hi in zip(BUCKET_EDGES, BUCKET_TOP)}
 
 
 def _run(nocc, nvirt, NBA, seed):

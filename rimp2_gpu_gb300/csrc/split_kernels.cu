@@ -2,9 +2,9 @@
 //
 // Numerics (Ozaki-style integer slices carried in FP16):
 //   For every column c=(a,i) of Calpha(:,a,i) a power-of-two scale s_c is
-//   chosen so that |C*s_c| <= 255.5 and ||round(C*s_c)||_2 <= 2^12.  Then
+//   chosen so that |C*s_c| <= 2047.5 and ||round(C*s_c)||_2 <= 2^12.  Then
 //     C*s_c = S0 + R1 (+ R2)
-//   with S0 = round(C*s_c) an integer in [-256,256] (exact in FP16) and R1, R2
+//   with S0 = round(C*s_c) an integer in [-2048,2048] (exact in FP16) and R1, R2
 //   the FP16-rounded residuals.  The alpha contraction of two columns is
 //     g*s_a*s_b = sum S0a S0b  +  sum (S0a R1b + R1a S0b + R1a R1b [+ S0a R2b + R2a S0b])
 //   The first sum (accumulator L0) is a sum of integers whose every partial
@@ -198,7 +198,7 @@ __device__ __forceinline__ float bits_to_float_trunc(unsigned long long b, int a
   const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
   if (mag == 0) return 0.0f;
   const int ex = (int)(mag >> 52) - 1023 + add_exp;
-  if (ex < -126) return 0.0f;  // below float range: negligible against |C*s| <= 256
+  if (ex < -126) return 0.0f;  // below float range: negligible against |C*s| <= 2048
   if (ex > 127) return __uint_as_float(((uint32_t)(b >> 63) << 31) | 0x7F800000u);
   const uint32_t mant = (uint32_t)((mag >> 29) & 0x7FFFFFu);
   const uint32_t sign = (uint32_t)(b >> 63) << 31;
@@ -300,12 +300,12 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
     // float truncation of the squares underestimates ||C||^2 by < 2^-21
     // relative; the exact integer check below keeps the exactness guarantee
     const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
-    const double lim = fmin(255.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / nrm);
+    const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / nrm);
     e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
     e = max(-100, min(100, e));
   }
   for (int attempt = 0; attempt < 64; ++attempt) {
-    int n2 = 0;  // sum of S0^2 (integers; <= 2^24 is the test)
+    long long n2 = 0;  // sum of S0^2 (integers; <= 2^24 is the test)
     for (int k = lane; k < Kpad; k += 32) {
       __half h0 = hz, h1 = hz, h2 = hz;
       if (k < NBA) {
@@ -313,11 +313,11 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
         split_double(c[k], e, xh, xl);
         const float q = rintf(xh);
         const float r = (xh - q) + xl;  // xh - q exact
-        h0 = __float2half_rn(q);        // integer |q| <= 256: exact
+        h0 = __float2half_rn(q);        // integer |q| <= 2048: exact in FP16
         h1 = __float2half_rn(r);
         h2 = __float2half_rn(r - __half2float(h1));
         const int qi = (int)q;
-        n2 += qi * qi;
+        n2 += (long long)qi * qi;
       }
       const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
       out[o] = h0;
@@ -326,7 +326,7 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
-    if (n2 <= 16777216) break;  // ||S0||^2 <= 2^24: L0 accumulation exact
+    if (n2 <= 16777216LL) break;  // ||S0||^2 <= 2^24: L0 accumulation exact
     --e;
   }
   if (lane == 0) inv_scale[F.col_base + col] = ldexpf(1.0f, -e);
