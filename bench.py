@@ -156,7 +156,7 @@ def traffic_per_launch():
         return None
     with open(p) as f:
         d = json.load(f)
-    return d.get("scaled_bytes_per_launch_full_workload")
+    return d.get("bytes_per_launch_full_workload")
 
 
 # ------------------------------------------------------------------------------------------
@@ -391,7 +391,9 @@ def run_ours(args):
     n_pairs_full = NOCC * (NOCC - 1) // 2
     ntile = (NVIRT + 127) // 128
     ntp = ntile * (ntile + 1) // 2
-    tiles = (2 * n_pairs_full + NOCC) * ntp
+    # i<j pairs: two 128x128 tiles per off-diagonal tile pair, one per diagonal
+    # tile pair (T2 = T1^T); i=j pairs: one tile per tile pair
+    tiles = n_pairs_full * (2 * (ntp - ntile) + ntile) + NOCC * ntp
     kpad = (NBA + 63) // 64 * 64
     performed = tiles * 128 * 128 * kpad * 2.0 * (4 if nsl == 1 else 6)
     roof = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",

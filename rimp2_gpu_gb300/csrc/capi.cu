@@ -3,6 +3,7 @@
 // codes and error strings.  All arithmetic happens in the kernels of
 // fp64_kernels.cu, split_kernels.cu and front_end.cu; there is no host
 // compute path.
+#include <algorithm>
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
@@ -123,6 +124,13 @@ int ensure_device() {
 }
 
 cudaStream_t current_stream() { return g_user_stream ? g_user_stream : g_lib_stream; }
+
+static cudaStream_t g_copy_stream = nullptr;
+cudaStream_t copy_stream() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_copy_stream) cudaStreamCreateWithFlags(&g_copy_stream, cudaStreamNonBlocking);
+  return g_copy_stream;
+}
 
 }  // namespace rimp2
 
@@ -816,6 +824,38 @@ int rimp2_energy(const int *nvirt, const int *nocc, const int *NBA, const double
   cudaStream_t s = current_stream();
   const size_t nv = *nvirt, no = *nocc, nb = *NBA;
   DevBuf dC, deo, dev, dE, dT, dA;
+  if (*precision == RIMP2_PREC_SPLIT) {
+    // copy Calpha in occupied-index chunks overlapped with the energy work
+    cudaStream_t cs = copy_stream();
+    RIMP2_REQ(cs != nullptr, "rimp2_energy: copy stream unavailable");
+    RIMP2_TRY(dalloc(dC, nb * nv * no, s));
+    RIMP2_TRY(h2d(deo, EVocc, no, s));
+    RIMP2_TRY(h2d(dev, EVvirt, nv, s));
+    RIMP2_TRY(dalloc(dE, no * no, s));
+    RIMP2_TRY(dalloc(dT, 1, s));
+    // the copy stream must see dC allocated before it writes into it
+    cudaEvent_t ready;
+    RIMP2_CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    RIMP2_CK(cudaEventRecord(ready, s));
+    RIMP2_CK(cudaStreamWaitEvent(cs, ready, 0));
+    cudaEventDestroy(ready);
+    SplitEnergyArgs a;
+    a.Ca = dC.as<double>();
+    a.NBA = *NBA;
+    a.nvirt = *nvirt;
+    a.nocc = *nocc;
+    a.eo = deo.as<double>();
+    a.ev = dev.as<double>();
+    a.Epair = dE.as<double>();
+    a.Etot = dT.as<double>();
+    a.nslices = rimp2_split_nslices(*nvirt, *nocc, *NBA);
+    const int chunk = std::max(1, std::min(16, (*nocc + 7) / 8));
+    RIMP2_TRY(split_energy_streamed(Calpha, dC.as<double>(), a, s, cs, chunk));
+    RIMP2_TRY(d2h(Epair, dE, no * no, s));
+    RIMP2_TRY(d2h(Etot, dT, 1, s));
+    RIMP2_CK(cudaStreamSynchronize(cs));
+    return finish(s);
+  }
   RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
   RIMP2_TRY(h2d(deo, EVocc, no, s));
   RIMP2_TRY(h2d(dev, EVvirt, nv, s));

@@ -121,6 +121,9 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
 int split_plan_execute(SplitPlan *P, cudaStream_t s);
 void split_plan_destroy(SplitPlan *P);
 int bounded_wait_selftest(long long budget_cycles, cudaStream_t s);
+int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs &a,
+                          cudaStream_t s, cudaStream_t copy_s, int chunk_occ);
+cudaStream_t copy_stream();
 bool split_supported();
 
 }  // namespace rimp2

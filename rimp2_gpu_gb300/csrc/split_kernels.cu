@@ -259,11 +259,13 @@ __device__ __forceinline__ void decode_pair(int p, int &i, int &j) {
 // K-chunk-major layout shared by all fragments (one tensor map per batch).
 // grid.y = fragment, one warp per column.
 __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, long long plane,
-                                   __half *__restrict__ slices, float *__restrict__ inv_scale) {
+                                   __half *__restrict__ slices, float *__restrict__ inv_scale,
+                                   int col0, int col1) {
+  // columns [col0, min(col1, ncol)) of each fragment
   const FragDesc &F = fr[blockIdx.y];
-  const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int col = col0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (col >= F.ncol) return;
+  if (col >= F.ncol || col >= col1) return;
   const int a = col % F.nvpad, i = col / F.nvpad;
   const int Kpad = F.nks * 64;
   const __half hz = __float2half_rn(0.0f);
@@ -369,7 +371,8 @@ __global__ void build_items_kernel(const FragDesc *__restrict__ fr, int nfrag, l
 struct BatchParams {
   const FragDesc *frags;
   const int4 *items;
-  long long nitems;
+  long long nitems;       // this launch drains items [item_begin, nitems)
+  long long item_begin;
   unsigned int *queue;     // next item counter (reset per launch)
   const float2 *eo2, *ev2;
   const float *inv_scale;
@@ -449,8 +452,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       bool ok = true;
       while (ok) {
         if (!mbar_wait(iempty0 + 8 * islot, iphase ^ 1, abort_flag, P.err, 5)) break;
-        const unsigned int id = atomicAdd(P.queue, 1u);
-        const int qidx = (long long)id < P.nitems ? (int)id : -1;
+        const long long id = P.item_begin + (long long)atomicAdd(P.queue, 1u);
+        const int qidx = id < P.nitems ? (int)id : -1;
         item_q[islot] = qidx;
         mbar_arrive(ifull0 + 8 * islot);
         if (++islot == IQ) {
@@ -942,7 +945,7 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
   {
     dim3 grid((unsigned)((g.max_ncol * 32LL + 255) / 256), (unsigned)g.nfrag);
     slice_batch_kernel<<<grid, 256, 0, s>>>(fr, g.nsl, g.R * 64, g.slices.as<__half>(),
-                                            g.inv.as<float>());
+                                            g.inv.as<float>(), 0, 0x7fffffff);
     dim3 g2((unsigned)((g.max_nv + 255) / 256), (unsigned)g.nfrag);
     eps_batch_kernel<<<g2, 256, 0, s>>>(fr, g.eo2.as<float2>(), g.ev2.as<float2>());
     count_launch(2);
@@ -952,6 +955,7 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
   P.frags = fr;
   P.items = g.items.as<int4>();
   P.nitems = g.nitems;
+  P.item_begin = 0;
   P.queue = g.queue.as<unsigned int>();
   P.eo2 = g.eo2.as<float2>();
   P.ev2 = g.ev2.as<float2>();
@@ -1088,6 +1092,110 @@ int bounded_wait_selftest(long long budget_cycles, cudaStream_t s) {
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   return collect_device_error(s);
+}
+
+// Host Calpha -> energies with the copy overlapped: occupied indices are
+// copied in chunks on a second stream; once chunk c has landed, its columns
+// are sliced and the work items of every pair (i <= j) with j in chunk c --
+// whose inputs are then all on the device -- run as one persistent launch,
+// while chunk c+1 is still in flight.  dCa must have room for the fragment.
+int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs &a,
+                          cudaStream_t s, cudaStream_t copy_s, int chunk_occ) {
+  if (inject_fault("launch")) {  // before any copy is in flight
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  SplitPlan *P = nullptr;
+  const int ns = a.nslices;
+  const double *dCaC = dCa;
+  RIMP2_TRY(split_plan_create(&P, 1, &a.nocc, &a.nvirt, &a.NBA, &dCaC, &a.eo, &a.ev, &a.Epair,
+                              &a.Etot, &ns, false, s));
+  Group &g = P->g[ns >= 2 ? 1 : 0];
+  const FragDesc &F = g.fh[0];
+  const FragDesc *fr = g.frags.as<FragDesc>();
+  int rc = RIMP2_OK;
+  const int nchunk = (a.nocc + chunk_occ - 1) / chunk_occ;
+  std::vector<cudaEvent_t> ev(nchunk);
+  for (auto &e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  const size_t slab = (size_t)a.NBA * a.nvirt;  // doubles per occupied index
+  // copies first, so the copy engine runs ahead of the compute stream
+  for (int c = 0; c < nchunk && rc == RIMP2_OK; ++c) {
+    const int i0 = c * chunk_occ, i1 = std::min(a.nocc, i0 + chunk_occ);
+    cudaError_t e = cudaMemcpyAsync(dCa + slab * i0, hCa + slab * i0, sizeof(double) * slab * (i1 - i0),
+                                    cudaMemcpyHostToDevice, copy_s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[c], copy_s);
+    if (e != cudaSuccess) {
+      set_error("streamed copy failed: %s", cudaGetErrorString(e));
+      rc = RIMP2_ERR_CUDA;
+    }
+  }
+  if (rc == RIMP2_OK) {
+    dim3 g2((unsigned)((g.max_nv + 255) / 256), 1);
+    eps_batch_kernel<<<g2, 256, 0, s>>>(fr, g.eo2.as<float2>(), g.ev2.as<float2>());
+    count_launch(1);
+  }
+  BatchParams BP;
+  BP.frags = fr;
+  BP.items = g.items.as<int4>();
+  BP.eo2 = g.eo2.as<float2>();
+  BP.ev2 = g.ev2.as<float2>();
+  BP.inv_scale = g.inv.as<float>();
+  BP.part = g.part.as<double>();
+  BP.err = device_error_word();
+  for (int c = 0; c < nchunk && rc == RIMP2_OK; ++c) {
+    const int i0 = c * chunk_occ, i1 = std::min(a.nocc, i0 + chunk_occ);
+    cudaError_t e = cudaStreamWaitEvent(s, ev[c], 0);
+    if (e != cudaSuccess) {
+      set_error("stream wait failed: %s", cudaGetErrorString(e));
+      rc = RIMP2_ERR_CUDA;
+      break;
+    }
+    const int col0 = i0 * F.nvpad, col1 = i1 * F.nvpad;
+    slice_batch_kernel<<<(unsigned)(((long long)(col1 - col0) * 32 + 255) / 256), 256, 0, s>>>(
+        fr, g.nsl, g.R * 64, g.slices.as<__half>(), g.inv.as<float>(), col0, col1);
+    // pairs (i<=j) with j in [i0, i1): pair indices [i0(i0+1)/2, i1(i1+1)/2)
+    const long long pb = (long long)i0 * (i0 + 1) / 2, pe = (long long)i1 * (i1 + 1) / 2;
+    BP.item_begin = pb * F.ntp;
+    BP.nitems = pe * F.ntp;
+    e = cudaMemsetAsync(g.queue.p, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) {
+      set_error("queue reset failed: %s", cudaGetErrorString(e));
+      rc = RIMP2_ERR_CUDA;
+      break;
+    }
+    BP.queue = g.queue.as<unsigned int>();
+    const int grid = (int)std::min<long long>(BP.nitems - BP.item_begin, P->nsm);
+    if (g.nsl == 2)
+      split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, BP);
+    else
+      split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, BP);
+    count_launch(2);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error("split launch failed: %s", cudaGetErrorString(e));
+      rc = RIMP2_ERR_CUDA;
+    }
+  }
+  if (rc == RIMP2_OK) {
+    pair_reduce_batch_kernel<<<(unsigned)((g.npairs_total + 7) / 8), 256, 0, s>>>(
+        fr, g.nfrag, g.npairs_total, g.part.as<double>());
+    total_reduce_batch_kernel<<<g.nfrag, 1024, 0, s>>>(fr);
+    count_launch(2);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error("reduction launch failed: %s", cudaGetErrorString(e));
+      rc = RIMP2_ERR_CUDA;
+    }
+  }
+  // on failure, copies may still be in flight into dCa: finish them before
+  // the caller can release dCa
+  if (rc != RIMP2_OK) {
+    cudaStreamSynchronize(copy_s);
+    cudaStreamSynchronize(s);
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  split_plan_destroy(P);
+  return rc;
 }
 
 int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {
