@@ -51,7 +51,12 @@ WORKLOAD = (f"split-precision RI-MP2 energy of one fragment nocc={NOCC} nvirt={N
 AO_N_DEFAULT = 64
 
 
-def eff_flop(nocc=NOCC, nvirt=NVIRT, nba=NBA):
+def eff_flop(nocc=None, nvirt=None, nba=None):
+    """Algorithmic FLOP of one fragment (sizes default to the current workload,
+    read at call time so command-line overrides apply)."""
+    nocc = NOCC if nocc is None else nocc
+    nvirt = NVIRT if nvirt is None else nvirt
+    nba = NBA if nba is None else nba
     return 2.0 * nba * (nocc * nvirt) ** 2
 
 

@@ -28,7 +28,7 @@ def test_bench_json_line_small_fragment():
     assert d["value"] > 0 and d["unit"] == "TFLOP/s" and d["steps"] == 2
     assert d["config"]["workload"]
     rf = d["roofline"]
-    assert rf["bound"] == "tensor" and 0 < rf["frac"] < 1.2 and rf["achieved"] > 0
+    assert rf["bound"] == "tensor" and 0 < rf["frac"] < 1.2 and rf["achieved"] > 0, rf
     assert d["e2e"]["h2d_bytes_per_step"] == 8 * (512 * 256 * 8 + 8 + 256)
     assert d["gpu_launches"] >= 2
     assert d["accuracy"]["within_1e-7"]
