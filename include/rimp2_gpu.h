@@ -230,6 +230,12 @@ int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc, const
  * positive-definiteness is checked before the solve). */
 int rimp2_calpha_from_ao_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao,
                              const double *dV, const double *dCmo, double *dCalpha, void *stream);
+/* Same, with the AO->MO transform on the tcgen05 tensor cores (exact-integer
+ * FP16 slices with two residual slices, ~2^-33 relative per product); the
+ * metric Cholesky and the triangular solve stay FP64. */
+int rimp2_calpha_from_ao_split_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao,
+                                   const double *dV, const double *dCmo, double *dCalpha,
+                                   void *stream);
 /* Building blocks: lower Cholesky V = L L^T in place (n x n, strict upper
  * zeroed; RIMP2_ERR_ARG if not positive definite) and X = L^{-1} B
  * (B n x m, overwritten as workspace; X separate). FP64, blocked, GPU. */

@@ -65,6 +65,8 @@ SIGNATURES = {
     "rimp2_calpha_from_ao": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp], C.c_int),
     "rimp2_calpha_from_ao_dev": ([C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp],
                                  C.c_int),
+    "rimp2_calpha_from_ao_split_dev": ([C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp,
+                                        _vp], C.c_int),
     "rimp2_cholesky_dev": ([C.c_int, _vp, _vp], C.c_int),
     "rimp2_trsm_lower_dev": ([C.c_int, C.c_int, _vp, _vp, _vp, _vp], C.c_int),
     "rimp2_gen_ao_dev": ([C.c_ulonglong, C.c_int, C.c_int, _vp, _vp, _vp], C.c_int),

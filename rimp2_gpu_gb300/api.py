@@ -251,6 +251,12 @@ def calpha_from_ao_dev(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, stream=0)
          stream or None)
 
 
+def calpha_from_ao_split_dev(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, stream=0):
+    """AO->MO transform on the tensor cores (split precision), FP64 Cholesky/solve."""
+    call("rimp2_calpha_from_ao_split_dev", NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha,
+         stream or None)
+
+
 def cholesky_dev(n, dV, stream=0):
     call("rimp2_cholesky_dev", n, dV, stream or None)
 

@@ -124,6 +124,21 @@ int bounded_wait_selftest(long long budget_cycles, cudaStream_t s);
 int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs &a,
                           cudaStream_t s, cudaStream_t copy_s, int chunk_occ);
 cudaStream_t copy_stream();
+// K-major FP16 slices of a set of rows (split GEMM operand)
+struct SlicedOp {
+  int nsl = 2, nks = 0;
+  long long rows_per_group = 0, ncol = 0, R = 0;
+  DevBuf slices, inv, desc;
+};
+// rows = columns of a column-major array: group g, row r at src + K*(r + nrows*g)
+int sliced_cols(SlicedOp &op, const double *src, int K, int nrows, int ngroups, int nsl,
+                cudaStream_t s);
+// rows m' = mu + nbas*alpha of (alpha|mu nu) over K = nu
+int sliced_ao(SlicedOp &op, const double *ao, int NBA, int nbas, int nsl, cudaStream_t s);
+// out[b*sOb + m*sOm + n*sOn] = sum_k A[a_row0 + b*a_bstride + m][k] * B[b_row0 + b*b_bstride + n][k]
+int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const SlicedOp &B,
+               long long b_row0, long long b_bstride, int M, int N, int nbatch, double *out,
+               long long sOm, long long sOn, long long sOb, cudaStream_t s);
 bool split_supported();
 
 }  // namespace rimp2

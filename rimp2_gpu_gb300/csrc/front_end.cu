@@ -257,14 +257,45 @@ int dev_ao2mo(int NBA, int nbas, int nocc, int nvirt, const double *ao, const do
   return RIMP2_OK;
 }
 
+// (alpha|a i) on the tcgen05 tensor cores with exact-integer FP16 slices
+// (S0 + two residual slices, ~2^-33 relative per product): the AO tensor is
+// sliced with K = nu contiguous (rows mu + nbas*alpha), contracted with the
+// occupied MO columns into half(i, alpha, mu), which is sliced again (rows
+// (alpha, i), K = mu) and contracted with the virtual MO columns, written in
+// the Calpha layout (alpha, a, i).
+int dev_ao2mo_split(int NBA, int nbas, int nocc, int nvirt, const double *ao, const double *Cmo,
+                    double *out, cudaStream_t s) {
+  const int nsl = 3;
+  const long long MK = (long long)NBA * nbas;
+  DevBuf half;
+  RIMP2_TRY(half.alloc(sizeof(double) * (size_t)MK * nocc, s));
+  {
+    SlicedOp Aao, Bocc;
+    RIMP2_TRY(sliced_ao(Aao, ao, NBA, nbas, nsl, s));
+    RIMP2_TRY(sliced_cols(Bocc, Cmo, nbas, nocc, 1, nsl, s));
+    // half[i][alpha][mu] = sum_nu ao(alpha,mu,nu) Cmo(nu,i); GEMM row m' = mu + nbas*alpha
+    RIMP2_TRY(split_gemm(Aao, 0, 0, Bocc, 0, 0, (int)MK, nocc, 1, half.as<double>(), 1, MK, 0, s));
+  }
+  SlicedOp Ah, Bv;
+  RIMP2_TRY(sliced_cols(Ah, half.as<double>(), nbas, NBA, nocc, nsl, s));
+  RIMP2_TRY(sliced_cols(Bv, Cmo + (size_t)nbas * nocc, nbas, nvirt, 1, nsl, s));
+  // out(alpha,a,i) = sum_mu half[i][alpha][mu] Cmo(mu,nocc+a)
+  RIMP2_TRY(split_gemm(Ah, 0, Ah.rows_per_group, Bv, 0, 0, NBA, nvirt, nocc, out, 1, NBA,
+                       (long long)NBA * nvirt, s));
+  return RIMP2_OK;
+}
+
 int dev_calpha_from_ao(int NBA, int nbas, int nocc, int nvirt, const double *ao, const double *V,
-                       const double *Cmo, double *Calpha, cudaStream_t s) {
+                       const double *Cmo, double *Calpha, cudaStream_t s, bool split_transform) {
   DevBuf L, B;
   RIMP2_TRY(L.alloc(sizeof(double) * (size_t)NBA * NBA, s));
   RIMP2_CK(cudaMemcpyAsync(L.p, V, sizeof(double) * (size_t)NBA * NBA, cudaMemcpyDeviceToDevice, s));
   RIMP2_TRY(dev_cholesky(NBA, L.as<double>(), s));
   RIMP2_TRY(B.alloc(sizeof(double) * (size_t)NBA * nvirt * nocc, s));
-  RIMP2_TRY(dev_ao2mo(NBA, nbas, nocc, nvirt, ao, Cmo, B.as<double>(), s));
+  if (split_transform)
+    RIMP2_TRY(dev_ao2mo_split(NBA, nbas, nocc, nvirt, ao, Cmo, B.as<double>(), s));
+  else
+    RIMP2_TRY(dev_ao2mo(NBA, nbas, nocc, nvirt, ao, Cmo, B.as<double>(), s));
   RIMP2_TRY(dev_trsm_lower(NBA, nvirt * nocc, L.as<double>(), B.as<double>(), Calpha, s));
   return RIMP2_OK;
 }
@@ -282,7 +313,19 @@ extern "C" int rimp2_calpha_from_ao_dev(int NBA, int nbas, int nocc, int nvirt, 
   RIMP2_REQ(dao && dV && dCmo && dCalpha, "rimp2_calpha_from_ao_dev: null array");
   RIMP2_TRY(ensure_device());
   cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
-  return dev_calpha_from_ao(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, s);
+  return dev_calpha_from_ao(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, s, false);
+}
+
+extern "C" int rimp2_calpha_from_ao_split_dev(int NBA, int nbas, int nocc, int nvirt,
+                                              const double *dao, const double *dV,
+                                              const double *dCmo, double *dCalpha, void *stream) {
+  clear_error();
+  RIMP2_REQ(NBA > 0 && nbas > 0 && nocc > 0 && nvirt > 0 && nocc + nvirt <= nbas,
+            "rimp2_calpha_from_ao_split_dev: bad dims (need nocc+nvirt <= nbas)");
+  RIMP2_REQ(dao && dV && dCmo && dCalpha, "rimp2_calpha_from_ao_split_dev: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  return dev_calpha_from_ao(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, s, true);
 }
 
 extern "C" int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc,
@@ -306,7 +349,7 @@ extern "C" int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *
   const size_t no = (size_t)nb * *nvirt * *nocc;
   RIMP2_TRY(dOut.alloc(sizeof(double) * no, s));
   RIMP2_TRY(dev_calpha_from_ao(*NBA, *nbas, *nocc, *nvirt, dao.as<double>(), dV.as<double>(),
-                               dC.as<double>(), dOut.as<double>(), s));
+                               dC.as<double>(), dOut.as<double>(), s, false));
   RIMP2_CK(cudaMemcpyAsync(Calpha, dOut.p, sizeof(double) * no, cudaMemcpyDeviceToHost, s));
   RIMP2_CK(cudaStreamSynchronize(s));
   RIMP2_CK(cudaGetLastError());

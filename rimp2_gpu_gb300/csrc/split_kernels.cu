@@ -149,6 +149,16 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b,
       : "memory");
 }
 
+__device__ __forceinline__ void mma_f16_id(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                           uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -982,6 +992,246 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
   return RIMP2_OK;
 }
 
+// ==========================================================================
+// General split-precision GEMM on the same slices (used by the AO->MO
+// transform): D[m][n] = sum_k A[m][k] B[n][k], A and B K-major FP16 slices
+// with per-row power-of-two scales, exact integer L0 + residual L1 in TMEM,
+// FP64 output (L0 and L1 combined in FP64) with arbitrary strides.
+// One output tile (128 x NT, NT <= 128) per CTA.
+// ==========================================================================
+struct GemmSP {
+  int M, N, NT, nks, mtiles, ntiles, nbatch;
+  long long a_ncol, b_ncol;        // rows per K chunk in each operand's slice layout
+  long long a_row0, a_bstride;     // first row of batch 0 and row stride between batches
+  long long b_row0, b_bstride;
+  const float *a_inv, *b_inv;      // per-row inverse scales (indexed like the rows)
+  double *out;
+  long long sOm, sOn, sOb;
+  uint32_t idesc;
+  int *err;
+};
+
+template <int NSL>
+__global__ void __launch_bounds__(192, 1)
+    split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      GemmSP P) {
+  constexpr int NST = 2;
+  constexpr int SLOT = PANEL_BYTES;                 // 16 KB per panel slot (A or B)
+  constexpr int STAGE_BYTES = NSL * 2 * SLOT;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(base + NST * STAGE_BYTES);  // full[2], empty[2], tfull, drain
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NST + 2);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[NST]);
+  const uint32_t tfull = smem_u32(&bars[2 * NST]), drain = smem_u32(&bars[2 * NST + 1]);
+  const int item = blockIdx.x;
+  const int b = item / (P.mtiles * P.ntiles);
+  const int rem = item % (P.mtiles * P.ntiles);
+  const int mt = rem / P.ntiles, nt = rem % P.ntiles;
+  const int stage_tx = NSL * (TILE * KSTEP * 2 + P.NT * KSTEP * 2);
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < NST; ++st) {
+      mbar_init(full0 + 8 * st, 1);
+      mbar_init(empty0 + 8 * st, 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const long long arow = P.a_row0 + (long long)b * P.a_bstride + (long long)mt * TILE;
+  const long long brow = P.b_row0 + (long long)b * P.b_bstride + (long long)nt * P.NT;
+  if (warp == 0) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int armed[NST] = {-1, -1};
+      bool ok = true;
+      for (int kc = 0; kc < P.nks; ++kc) {
+        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err, 11)) {
+          ok = false;
+          break;
+        }
+        const uint32_t fb = full0 + 8 * stage;
+        mbar_expect_tx(fb, stage_tx);
+        armed[stage] = (int)phase;
+        const uint32_t dst = smem_u32(base + stage * STAGE_BYTES);
+#pragma unroll
+        for (int sl = 0; sl < NSL; ++sl) {
+          tma_load_3d(dst + (2 * sl) * SLOT, &tmA, fb, 0, (int)(kc * P.a_ncol + arow), sl);
+          tma_load_3d(dst + (2 * sl + 1) * SLOT, &tmB, fb, 0, (int)(kc * P.b_ncol + brow), sl);
+        }
+        if (++stage == NST) {
+          stage = 0;
+          phase ^= 1;
+        }
+      }
+      if (!ok) {
+        for (int st = 0; st < NST; ++st) {
+          if (armed[st] < 0) continue;
+          const long long t0 = clock64();
+          while (!mbar_test(full0 + 8 * st, (uint32_t)armed[st]) && clock64() - t0 < WAIT_BUDGET) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      const uint32_t dL0 = tmem, dL1 = tmem + TILE;
+      for (int kc = 0; kc < P.nks; ++kc) {
+        if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err, 12)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t sb = smem_u32(base + stage * STAGE_BYTES);
+#pragma unroll
+        for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
+          const uint32_t koff = k16 * 32;
+          const uint64_t a0 = smem_desc(sb + 0 * SLOT + koff), b0 = smem_desc(sb + 1 * SLOT + koff);
+          const uint64_t a1 = smem_desc(sb + 2 * SLOT + koff), b1 = smem_desc(sb + 3 * SLOT + koff);
+          const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
+          mma_f16_id(dL0, a0, b0, P.idesc, acc);
+          mma_f16_id(dL1, a0, b1, P.idesc, acc);
+          mma_f16_id(dL1, a1, b0, P.idesc, 1u);
+          mma_f16_id(dL1, a1, b1, P.idesc, 1u);
+          if (NSL > 2) {
+            const uint64_t a2 = smem_desc(sb + 4 * SLOT + koff), b2 = smem_desc(sb + 5 * SLOT + koff);
+            mma_f16_id(dL1, a0, b2, P.idesc, 1u);
+            mma_f16_id(dL1, a2, b0, P.idesc, 1u);
+          }
+        }
+        mma_commit(empty0 + 8 * stage);
+        if (++stage == NST) {
+          stage = 0;
+          phase ^= 1;
+        }
+      }
+      if (ok) mma_commit(tfull);
+      mma_commit(drain);
+      const long long t0 = clock64();
+      while (!mbar_test(drain, 0) && clock64() - t0 < WAIT_BUDGET) {
+      }
+    }
+  } else {
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    const long long m = (long long)mt * TILE + row;
+    if (mbar_wait(tfull, 0, abort_flag, P.err, 13)) {
+      tc_fence_after();
+      const double sa = (double)P.a_inv[arow + row];
+      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16);
+      double *orow = P.out + (long long)b * P.sOb + m * P.sOm;
+      for (int c0 = 0; c0 < P.NT; c0 += 16) {
+        float l0[16], l1[16];
+        tmem_ld16(taddr + c0, l0);
+        tmem_ld16(taddr + TILE + c0, l1);
+        tmem_wait_ld();
+        if (m < P.M) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const int n = nt * P.NT + c0 + k;
+            if (c0 + k < P.NT && n < P.N) {
+              const double sb = (double)P.b_inv[brow + c0 + k];
+              orow[(long long)n * P.sOn] = ((double)l0[k] + (double)l1[k]) * (sa * sb);
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+  }
+}
+
+// AO tensor rows: row m' = mu + nbas*alpha of (alpha|mu nu) over K = nu, one
+// thread per row, threads ordered alpha-fastest so that every load of a
+// nu-step is coalesced.  Same scale rule and slice layout as slice_batch_kernel.
+__global__ void ao_slice_kernel(const double *__restrict__ ao, int NBA, int nbas, long long nrows_pad,
+                                int nks, int nsl, long long plane, __half *__restrict__ slices,
+                                float *__restrict__ inv_scale) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long MK = (long long)NBA * nbas;
+  if (t >= nrows_pad) return;
+  const __half hz = __float2half_rn(0.0f);
+  const size_t kstride = (size_t)nrows_pad * 64;
+  if (t >= MK) {  // padding rows
+    __half *out = slices + (size_t)t * 64;
+    for (int kc = 0; kc < nks; ++kc)
+      for (int q = 0; q < 64; ++q)
+        for (int sl = 0; sl < nsl; ++sl) out[sl * plane + kc * kstride + q] = hz;
+    inv_scale[t] = 1.0f;
+    return;
+  }
+  const int al = (int)(t % NBA), mu = (int)(t / NBA);
+  const long long row = (long long)mu + (long long)nbas * al;
+  const double *src = ao + al + (size_t)NBA * mu;  // element nu at src[MK*nu]
+  unsigned long long mxb = 0;
+  float ss = 0.0f;
+  for (int nu = 0; nu < nbas; ++nu) {
+    const unsigned long long bb = (unsigned long long)__double_as_longlong(src[(size_t)MK * nu]);
+    const unsigned long long mag = bb & 0x7FFFFFFFFFFFFFFFull;
+    mxb = mag > mxb ? mag : mxb;
+    const float f = bits_to_float_trunc(mag, 0);
+    ss = fmaf(f, f, ss);
+  }
+  const double mx = __longlong_as_double((long long)mxb);
+  int e = 0;
+  if (mx > 0.0) {
+    const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
+    const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)nbas)) / nrm);
+    e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
+    e = max(-100, min(100, e));
+  }
+  __half *out = slices + (size_t)row * 64;
+  for (int attempt = 0; attempt < 64; ++attempt) {
+    long long n2 = 0;
+    for (int kc = 0; kc < nks; ++kc) {
+      for (int q = 0; q < 64; ++q) {
+        const int nu = kc * 64 + q;
+        __half h0 = hz, h1 = hz, h2 = hz;
+        if (nu < nbas) {
+          float xh, xl;
+          split_double(src[(size_t)MK * nu], e, xh, xl);
+          const float qv = rintf(xh);
+          const float r = (xh - qv) + xl;
+          h0 = __float2half_rn(qv);
+          h1 = __float2half_rn(r);
+          h2 = __float2half_rn(r - __half2float(h1));
+          const int qi = (int)qv;
+          n2 += (long long)qi * qi;
+        }
+        const size_t o = (size_t)kc * kstride + q;
+        out[o] = h0;
+        if (nsl > 1) out[plane + o] = h1;
+        if (nsl > 2) out[2 * plane + o] = h2;
+      }
+    }
+    if (n2 <= 16777216LL) break;
+    --e;
+  }
+  inv_scale[row] = ldexpf(1.0f, -e);
+}
+
 }  // namespace
 
 // A planned batch: up to two slice-count groups, workspace and (optionally)
@@ -1196,6 +1446,132 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   for (auto &e : ev) cudaEventDestroy(e);
   split_plan_destroy(P);
   return rc;
+}
+
+// ---- general split GEMM: host side -------------------------------------------
+int sliced_cols(SlicedOp &op, const double *src, int K, int nrows, int ngroups, int nsl,
+                cudaStream_t s) {
+  FragDesc F;
+  memset(&F, 0, sizeof F);
+  F.nocc = ngroups;
+  F.nvirt = nrows;
+  F.NBA = K;
+  F.nvpad = (nrows + TILE - 1) / TILE * TILE;
+  F.nks = (K + KSTEP - 1) / KSTEP;
+  F.ncol = ngroups * F.nvpad;
+  F.Ca = src;
+  op.nsl = nsl;
+  op.nks = F.nks;
+  op.rows_per_group = F.nvpad;
+  op.ncol = F.ncol;
+  op.R = (long long)F.nks * F.ncol;
+  if (op.R > 2147483647LL - TILE) {
+    set_error("split GEMM operand too large (%lld rows)", op.R);
+    return RIMP2_ERR_ARG;
+  }
+  RIMP2_TRY(op.desc.alloc(sizeof(FragDesc), s));
+  RIMP2_CK(cudaMemcpyAsync(op.desc.p, &F, sizeof F, cudaMemcpyHostToDevice, s));
+  RIMP2_TRY(op.slices.alloc(sizeof(__half) * (size_t)nsl * op.R * 64, s));
+  RIMP2_TRY(op.inv.alloc(sizeof(float) * (size_t)op.ncol, s));
+  slice_batch_kernel<<<(unsigned)(((long long)F.ncol * 32 + 255) / 256), 256, 0, s>>>(
+      op.desc.as<FragDesc>(), nsl, op.R * 64, op.slices.as<__half>(), op.inv.as<float>(), 0,
+      0x7fffffff);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+int sliced_ao(SlicedOp &op, const double *ao, int NBA, int nbas, int nsl, cudaStream_t s) {
+  const long long rows = (long long)NBA * nbas;
+  op.nsl = nsl;
+  op.nks = (nbas + KSTEP - 1) / KSTEP;
+  op.ncol = (rows + TILE - 1) / TILE * TILE;
+  op.rows_per_group = op.ncol;
+  op.R = (long long)op.nks * op.ncol;
+  if (op.R > 2147483647LL - TILE) {
+    set_error("AO operand too large (%lld rows)", op.R);
+    return RIMP2_ERR_ARG;
+  }
+  RIMP2_TRY(op.slices.alloc(sizeof(__half) * (size_t)nsl * op.R * 64, s));
+  RIMP2_TRY(op.inv.alloc(sizeof(float) * (size_t)op.ncol, s));
+  ao_slice_kernel<<<(unsigned)((op.ncol + 127) / 128), 128, 0, s>>>(
+      ao, NBA, nbas, op.ncol, op.nks, nsl, op.R * 64, op.slices.as<__half>(), op.inv.as<float>());
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+static int encode_op(CUtensorMap &tm, const SlicedOp &op, int boxrows) {
+  auto encode = get_encode();
+  if (!encode) {
+    set_error("cuTensorMapEncodeTiled entry point unavailable");
+    return RIMP2_ERR_UNSUPPORTED;
+  }
+  cuuint64_t dims[3] = {64, (cuuint64_t)op.R, (cuuint64_t)op.nsl};
+  cuuint64_t strides[2] = {128, (cuuint64_t)op.R * 128};
+  cuuint32_t box[3] = {KSTEP, (cuuint32_t)boxrows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult cr = encode(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, op.slices.p, dims, strides, box,
+                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+    return RIMP2_ERR_CUDA;
+  }
+  return RIMP2_OK;
+}
+
+int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const SlicedOp &B,
+               long long b_row0, long long b_bstride, int M, int N, int nbatch, double *out,
+               long long sOm, long long sOn, long long sOb, cudaStream_t s) {
+  if (A.nsl != B.nsl || A.nks != B.nks || M <= 0 || N <= 0 || nbatch <= 0) {
+    set_error("split_gemm: operand mismatch or bad sizes");
+    return RIMP2_ERR_ARG;
+  }
+  GemmSP P;
+  memset(&P, 0, sizeof P);
+  P.M = M;
+  P.N = N;
+  P.NT = N <= TILE ? (N + 15) / 16 * 16 : TILE;
+  P.nks = A.nks;
+  P.mtiles = (M + TILE - 1) / TILE;
+  P.ntiles = (N + P.NT - 1) / P.NT;
+  P.nbatch = nbatch;
+  P.a_ncol = A.ncol;
+  P.b_ncol = B.ncol;
+  P.a_row0 = a_row0;
+  P.a_bstride = a_bstride;
+  P.b_row0 = b_row0;
+  P.b_bstride = b_bstride;
+  P.a_inv = A.inv.as<float>();
+  P.b_inv = B.inv.as<float>();
+  P.out = out;
+  P.sOm = sOm;
+  P.sOn = sOn;
+  P.sOb = sOb;
+  P.idesc = (1u << 4) | ((uint32_t)(P.NT >> 3) << 17) | ((uint32_t)(TILE >> 4) << 24);
+  P.err = device_error_word();
+  const long long nitems = (long long)nbatch * P.mtiles * P.ntiles;
+  if (nitems > 2147483647LL) {
+    set_error("split_gemm: too many tiles");
+    return RIMP2_ERR_ARG;
+  }
+  CUtensorMap tA, tB;
+  RIMP2_TRY(encode_op(tA, A, TILE));
+  RIMP2_TRY(encode_op(tB, B, P.NT));
+  const int smem = 2 * A.nsl * 2 * PANEL_BYTES + 1024 + 256;
+  if (A.nsl == 3) {
+    RIMP2_CK(cudaFuncSetAttribute(split_gemm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem));
+    split_gemm_kernel<3><<<(unsigned)nitems, 192, smem, s>>>(tA, tB, P);
+  } else {
+    RIMP2_CK(cudaFuncSetAttribute(split_gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem));
+    split_gemm_kernel<2><<<(unsigned)nitems, 192, smem, s>>>(tA, tB, P);
+  }
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
 }
 
 int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel) {

@@ -80,3 +80,36 @@ def test_cholesky_rejects_indefinite_metric():
         api.cholesky_dev(n, dV.data_ptr())
     assert ei.value.status == 1 and "positive definite" in str(ei.value)
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("NBA,nbas,nocc", [(96, 40, 4), (300, 130, 13), (200, 77, 7)])
+def test_split_ao2mo_matches_fp64(NBA, nbas, nocc):
+    """AO->MO on the tensor cores (exact-integer FP16 slices, two residual
+    slices) against the FP64 front end on the same inputs: Calpha within
+    1e-8 of its largest element (the FP64 solve by the metric's Cholesky
+    factor amplifies the transform's ~1e-10 rounding a few times), energies
+    within 1e-7."""
+    import torch
+    from rimp2_gpu_gb300 import api
+    nvirt = nbas - nocc
+    dao = torch.zeros(NBA * nbas * nbas, dtype=torch.float64, device="cuda")
+    dV = torch.zeros(NBA * NBA, dtype=torch.float64, device="cuda")
+    api.gen_ao_dev(11, NBA, nbas, dao.data_ptr(), dV.data_ptr())
+    dC = t(O.gen_mo(11, nbas))
+    out64 = torch.zeros(NBA * nvirt * nocc, dtype=torch.float64, device="cuda")
+    outsp = torch.zeros_like(out64)
+    api.calpha_from_ao_dev(NBA, nbas, nocc, nvirt, dao.data_ptr(), dV.data_ptr(), dC.data_ptr(),
+                           out64.data_ptr())
+    api.calpha_from_ao_split_dev(NBA, nbas, nocc, nvirt, dao.data_ptr(), dV.data_ptr(),
+                                 dC.data_ptr(), outsp.data_ptr())
+    torch.cuda.synchronize()
+    a, b = outsp.cpu().numpy(), out64.cpu().numpy()
+    close(a, b, 1e-8)
+    eo = np.sort(np.linspace(-1.3, -0.4, nocc))
+    ev = np.sort(np.linspace(0.2, 2.8, nvirt))
+    Ca64 = b.reshape(NBA, nvirt, nocc, order="F")
+    Casp = np.asfortranarray(a.reshape(NBA, nvirt, nocc, order="F"))
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, np.asfortranarray(Ca64), eo, ev, blocked=True)
+    Ep, E = api.energy(nvirt, nocc, NBA, Casp, eo, ev, precision=api.PREC_SPLIT)
+    assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 1e-7
+    assert abs(E - Er) <= 1e-7 * abs(Er)
