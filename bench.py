@@ -76,6 +76,9 @@ def parse():
                          "batched: 256 uneven fragments in one graph-launched persistent kernel")
     ap.add_argument("--ao-fragments", type=int, default=AO_N_DEFAULT,
                     help="fragments in the AO pipeline workload")
+    ap.add_argument("--ao-transform", choices=["split", "fp64"], default="split",
+                    help="AO->MO transform on the tensor cores (split) or in FP64; the metric "
+                         "Cholesky and the triangular solve are FP64 either way")
     ap.add_argument("--nocc", type=int, default=None, help="override (profiling small cases)")
     ap.add_argument("--nvirt", type=int, default=None)
     ap.add_argument("--nba", type=int, default=None)
@@ -589,9 +592,11 @@ def run_ao(args):
     shapes = ao_shapes(args.ao_fragments)
     maxao = max(b * b * nba for b, nba, _, _ in shapes)
     maxv = max(nba * nba for _, nba, _, _ in shapes)
+    maxb = max(nba * nvirt * nocc for _, nba, nocc, nvirt in shapes)
     with torch.cuda.stream(st):
         ao = torch.empty(maxao, dtype=torch.float64, device=dev)
         V = torch.empty(maxv, dtype=torch.float64, device=dev)
+        Bw = torch.empty(maxb, dtype=torch.float64, device=dev)  # (alpha|a i) work array
     frags, desc, cmos = [], [], []
     for f, (nbas, nba, nocc, nvirt) in enumerate(shapes):
         with torch.cuda.stream(st):
@@ -609,26 +614,41 @@ def run_ao(args):
     st.synchronize()
     plan = None
     fe_ms, en_ms = [], []
-    front_flop = sum(2.0 * nba * nbas * nbas * nocc + 2.0 * nba * nbas * nvirt * nocc
-                     + 1.0 * nba * nba * nvirt * nocc + nba ** 3 / 1.5
-                     for nbas, nba, nocc, nvirt in shapes)
-    ao_bytes = sum(8.0 * nba * nbas * nbas for nbas, nba, _, _ in shapes)
+    tr_flop = sum(2.0 * nba * nbas * nbas * nocc + 2.0 * nba * nbas * nvirt * nocc
+                  for nbas, nba, nocc, nvirt in shapes)
+    so_flop = sum(1.0 * nba * nba * nvirt * nocc for nbas, nba, nocc, nvirt in shapes)
+    ch_flop = sum(nba ** 3 / 3.0 for _, nba, _, _ in shapes)
+    # algorithmic bytes of the transform: the AO tensor read once, (alpha|a i) written
+    ao_bytes = sum(8.0 * nba * nbas * nbas + 8.0 * nba * nvirt * nocc
+                   for nbas, nba, nocc, nvirt in shapes)
     eff = sum(2.0 * nba * (nocc * nvirt) ** 2 for _, nba, nocc, nvirt in shapes)
     n0 = None
+    parts_ms = []
     for step in range(args.warmup + args.steps):
         if step == args.warmup:
             n0 = api.kernel_launch_count()
         fe = 0.0
+        tr = ch = so = 0.0
         for f, (nbas, nba, nocc, nvirt) in enumerate(shapes):
             api.gen_ao_dev(4000 + f, nba, nbas, ao.data_ptr(), V.data_ptr(), stream=sp)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            api.calpha_from_ao_dev(nba, nbas, nocc, nvirt, ao.data_ptr(), V.data_ptr(),
-                                   frags[f]["Cmo"].data_ptr(), frags[f]["C"].data_ptr(), stream=sp)
-            e1.record(st)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(st)
+            # AO->MO transform (tensor cores or FP64), metric Cholesky, triangular solve
+            api.ao2mo_dev(nba, nbas, nocc, nvirt, ao.data_ptr(), frags[f]["Cmo"].data_ptr(),
+                          Bw.data_ptr(), split=(args.ao_transform == "split"), stream=sp)
+            ev[1].record(st)
+            api.cholesky_dev(nba, V.data_ptr(), stream=sp)
+            ev[2].record(st)
+            api.trsm_lower_dev(nba, nvirt * nocc, V.data_ptr(), Bw.data_ptr(),
+                               frags[f]["C"].data_ptr(), stream=sp)
+            ev[3].record(st)
             st.synchronize()
-            fe += e0.elapsed_time(e1)
+            tr += ev[0].elapsed_time(ev[1])
+            ch += ev[1].elapsed_time(ev[2])
+            so += ev[2].elapsed_time(ev[3])
+            fe += ev[0].elapsed_time(ev[3])
+        if step >= args.warmup:
+            parts_ms.append((tr, ch, so))
         if plan is None:
             plan = api.BatchPlan(desc, graph=True, stream=sp)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -643,6 +663,9 @@ def run_ao(args):
             en_ms.append(e0.elapsed_time(e1))
     launches = api.kernel_launch_count() - n0
     fe_m, en_m = statistics.median(fe_ms), statistics.median(en_ms)
+    tr_m = statistics.median(p[0] for p in parts_ms)
+    ch_m = statistics.median(p[1] for p in parts_ms)
+    so_m = statistics.median(p[2] for p in parts_ms)
     ms = allmax(pg, fe_m + en_m)
     acc = None
     if args.check == "full":
@@ -668,13 +691,19 @@ def run_ao(args):
             "metric": METRIC, "value": world * eff / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 front end; f16 Ozaki slices / f32 tensor accumulation for the energy",
+            "dtype": ("f16 Ozaki slices for AO->MO and the energy, f64 Cholesky/solve/reductions"
+                      if args.ao_transform == "split" else
+                      "f64 front end; f16 Ozaki slices / f32 tensor accumulation for the energy"),
             "data": "synthetic (device Philox AO integrals and metric, numpy QR MO coefficients)",
             "config": {"workload": f"pipeline from AO integrals, {len(shapes)} fragments "
                                    "(nbas U[128,768], NBA=3 nbas, nocc=nbas/10)",
+                       "ao_transform": args.ao_transform,
                        "front_end_ms": fe_m, "energy_ms": en_m,
-                       "front_end_fp64_tflops": front_flop / (fe_m * 1e-3) / 1e12,
-                       "ao_read_gbs": ao_bytes / (fe_m * 1e-3) / 1e9,
+                       "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,
+                       "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
+                       "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
+                       "cholesky_fp64_tflops": ch_flop / (ch_m * 1e-3) / 1e12,
+                       "solve_fp64_tflops": so_flop / (so_m * 1e-3) / 1e12,
                        "energy_eff_tflops": eff / (en_m * 1e-3) / 1e12,
                        "ao_generation": "untimed, per fragment, streamed through one buffer",
                        "parallelism": f"replicas x{world}"},

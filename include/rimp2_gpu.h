@@ -236,7 +236,11 @@ int rimp2_calpha_from_ao_dev(int NBA, int nbas, int nocc, int nvirt, const doubl
 int rimp2_calpha_from_ao_split_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao,
                                    const double *dV, const double *dCmo, double *dCalpha,
                                    void *stream);
-/* Building blocks: lower Cholesky V = L L^T in place (n x n, strict upper
+/* Building blocks: the AO->MO transform alone, (alpha|a i) in the Calpha
+ * layout (NBA,nvirt,nocc); split != 0 selects the tensor-core form. */
+int rimp2_ao2mo_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao, const double *dCmo,
+                    double *dout, int split, void *stream);
+/* Lower Cholesky V = L L^T in place (n x n, strict upper
  * zeroed; RIMP2_ERR_ARG if not positive definite) and X = L^{-1} B
  * (B n x m, overwritten as workspace; X separate). FP64, blocked, GPU. */
 int rimp2_cholesky_dev(int n, double *dV, void *stream);

@@ -67,6 +67,8 @@ SIGNATURES = {
                                  C.c_int),
     "rimp2_calpha_from_ao_split_dev": ([C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp,
                                         _vp], C.c_int),
+    "rimp2_ao2mo_dev": ([C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp],
+                        C.c_int),
     "rimp2_cholesky_dev": ([C.c_int, _vp, _vp], C.c_int),
     "rimp2_trsm_lower_dev": ([C.c_int, C.c_int, _vp, _vp, _vp, _vp], C.c_int),
     "rimp2_gen_ao_dev": ([C.c_ulonglong, C.c_int, C.c_int, _vp, _vp, _vp], C.c_int),

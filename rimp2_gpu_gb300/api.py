@@ -257,6 +257,12 @@ def calpha_from_ao_split_dev(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, str
          stream or None)
 
 
+def ao2mo_dev(NBA, nbas, nocc, nvirt, dao, dCmo, dout, split=True, stream=0):
+    """(alpha|a i) from (alpha|mu nu) and the MO coefficients, device pointers."""
+    call("rimp2_ao2mo_dev", NBA, nbas, nocc, nvirt, dao, dCmo, dout, 1 if split else 0,
+         stream or None)
+
+
 def cholesky_dev(n, dV, stream=0):
     call("rimp2_cholesky_dev", n, dV, stream or None)
 

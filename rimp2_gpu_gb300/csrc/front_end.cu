@@ -316,6 +316,18 @@ extern "C" int rimp2_calpha_from_ao_dev(int NBA, int nbas, int nocc, int nvirt, 
   return dev_calpha_from_ao(NBA, nbas, nocc, nvirt, dao, dV, dCmo, dCalpha, s, false);
 }
 
+extern "C" int rimp2_ao2mo_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao,
+                               const double *dCmo, double *dout, int split, void *stream) {
+  clear_error();
+  RIMP2_REQ(NBA > 0 && nbas > 0 && nocc > 0 && nvirt > 0 && nocc + nvirt <= nbas,
+            "rimp2_ao2mo_dev: bad dims (need nocc+nvirt <= nbas)");
+  RIMP2_REQ(dao && dCmo && dout, "rimp2_ao2mo_dev: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  return split ? dev_ao2mo_split(NBA, nbas, nocc, nvirt, dao, dCmo, dout, s)
+               : dev_ao2mo(NBA, nbas, nocc, nvirt, dao, dCmo, dout, s);
+}
+
 extern "C" int rimp2_calpha_from_ao_split_dev(int NBA, int nbas, int nocc, int nvirt,
                                               const double *dao, const double *dV,
                                               const double *dCmo, double *dCalpha, void *stream) {

@@ -1176,9 +1176,11 @@ __global__ void ao_slice_kernel(const double *__restrict__ ao, int NBA, int nbas
   const size_t kstride = (size_t)nrows_pad * 64;
   if (t >= MK) {  // padding rows
     __half *out = slices + (size_t)t * 64;
+    const uint4 z = make_uint4(0, 0, 0, 0);
     for (int kc = 0; kc < nks; ++kc)
-      for (int q = 0; q < 64; ++q)
-        for (int sl = 0; sl < nsl; ++sl) out[sl * plane + kc * kstride + q] = hz;
+      for (int q = 0; q < 64; q += 8)
+        for (int sl = 0; sl < nsl; ++sl)
+          *reinterpret_cast<uint4 *>(out + sl * plane + kc * kstride + q) = z;
     inv_scale[t] = 1.0f;
     return;
   }
@@ -1206,24 +1208,30 @@ __global__ void ao_slice_kernel(const double *__restrict__ ao, int NBA, int nbas
   for (int attempt = 0; attempt < 64; ++attempt) {
     long long n2 = 0;
     for (int kc = 0; kc < nks; ++kc) {
-      for (int q = 0; q < 64; ++q) {
-        const int nu = kc * 64 + q;
-        __half h0 = hz, h1 = hz, h2 = hz;
-        if (nu < nbas) {
-          float xh, xl;
-          split_double(src[(size_t)MK * nu], e, xh, xl);
-          const float qv = rintf(xh);
-          const float r = (xh - qv) + xl;
-          h0 = __float2half_rn(qv);
-          h1 = __float2half_rn(r);
-          h2 = __float2half_rn(r - __half2float(h1));
-          const int qi = (int)qv;
-          n2 += (long long)qi * qi;
+      // eight values at a time, written as one 16-byte store per slice
+      for (int q0 = 0; q0 < 64; q0 += 8) {
+        __align__(16) __half h0[8], h1[8], h2[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int nu = kc * 64 + q0 + q;
+          h0[q] = h1[q] = h2[q] = hz;
+          if (nu < nbas) {
+            float xh, xl;
+            split_double(src[(size_t)MK * nu], e, xh, xl);
+            const float qv = rintf(xh);
+            const float r = (xh - qv) + xl;
+            h0[q] = __float2half_rn(qv);
+            h1[q] = __float2half_rn(r);
+            h2[q] = __float2half_rn(r - __half2float(h1[q]));
+            const int qi = (int)qv;
+            n2 += (long long)qi * qi;
+          }
         }
-        const size_t o = (size_t)kc * kstride + q;
-        out[o] = h0;
-        if (nsl > 1) out[plane + o] = h1;
-        if (nsl > 2) out[2 * plane + o] = h2;
+        const size_t o = (size_t)kc * kstride + q0;
+        *reinterpret_cast<uint4 *>(out + o) = *reinterpret_cast<const uint4 *>(h0);
+        if (nsl > 1) *reinterpret_cast<uint4 *>(out + plane + o) = *reinterpret_cast<const uint4 *>(h1);
+        if (nsl > 2)
+          *reinterpret_cast<uint4 *>(out + 2 * plane + o) = *reinterpret_cast<const uint4 *>(h2);
       }
     }
     if (n2 <= 16777216LL) break;
