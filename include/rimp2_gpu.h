@@ -189,11 +189,14 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
                          double *Epair, const long long *epair_off, double *Etot,
                          const int *precision);
 
-/* Batched split-precision energies of many fragments of uneven size, all
- * resident on the device, in ONE persistent launch per slice-count group:
- * a device-side queue of (fragment, pair i<=j, tile pair) work items ordered
- * heaviest fragment first, drained by one CTA per SM.  With use_graph != 0
- * the whole evaluation (slicing, energy kernel, reductions) is captured once
+/* Batched energies of many fragments of uneven size, all resident on the
+ * device, in ONE persistent launch per slice-count group: a device-side
+ * queue of (fragment, pair i<=j, tile pair) work items ordered heaviest
+ * fragment first, drained by one CTA per SM.  nslices[f] = 1 or 2 runs
+ * fragment f in the split form with that many residual slices; 0 runs it in
+ * plain FP64 (the fused DMMA kernel's tile pairs, drained by one persistent
+ * launch over all FP64 fragments of the plan).  With use_graph != 0 the
+ * whole evaluation (slicing, energy kernels, reductions) is captured once
  * as a CUDA graph and every execute is one graph launch.  nslices may be NULL
  * (per-fragment choice from the shape-bucket table).  The plan keeps its
  * workspace until destroyed and reads the fragment pointers at every

@@ -190,12 +190,13 @@ def gen_fragment_dev(seed, nocc, nvirt, NBA, dCalpha=0, dEVocc=0, dEVvirt=0, str
 
 
 class BatchPlan:
-    """Batched split-precision energies of many device-resident fragments:
-    one persistent launch per slice-count group draining a device work
-    queue, optionally captured once as a CUDA graph (C-ABI
-    rimp2_batch_plan_*).  ``frags`` is a list of
-    (nocc, nvirt, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot) with device
-    addresses; outputs are written at every ``execute``."""
+    """Batched energies of many device-resident fragments: one persistent
+    launch per slice-count group draining a device work queue, optionally
+    captured once as a CUDA graph (C-ABI rimp2_batch_plan_*).  ``frags`` is
+    a list of (nocc, nvirt, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot)
+    with device addresses; ``nslices`` per fragment is 1 or 2 (split form)
+    or 0 (plain FP64), None for the shape-bucket table; outputs are written
+    at every ``execute``."""
 
     def __init__(self, frags, nslices=None, graph=True, stream=0):
         n = len(frags)

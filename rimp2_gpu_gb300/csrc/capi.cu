@@ -763,7 +763,8 @@ int rimp2_batch_plan_create(void **plan, int nfrag, const int *nocc, const int *
     RIMP2_REQ(dCalpha[f] && dEVocc[f] && dEVvirt[f] && dEpair[f] && dEtot[f],
               "rimp2_batch_plan_create: null device pointer in fragment %d", f);
     ns[f] = nslices ? nslices[f] : rimp2_split_nslices(nvirt[f], nocc[f], NBA[f]);
-    RIMP2_REQ(ns[f] == 1 || ns[f] == 2, "rimp2_batch_plan_create: nslices must be 1 or 2");
+    RIMP2_REQ(ns[f] >= 0 && ns[f] <= 2,
+              "rimp2_batch_plan_create: nslices must be 0 (FP64), 1 or 2");
   }
   RIMP2_TRY(ensure_device());
   cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
@@ -925,29 +926,18 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
     ov += nvirt[f];
     oe += (size_t)nocc[f] * nocc[f];
   }
-  if (*precision == RIMP2_PREC_SPLIT) {
+  {
+    // split: per-fragment slice count from the bucket table; FP64: every
+    // fragment in the plain persistent launch
+    std::vector<int> zeros(nf, 0);
     void *plan = nullptr;
     RIMP2_TRY(rimp2_batch_plan_create(&plan, nf, nocc, nvirt, NBA, pc.data(), peo.data(),
-                                      pev.data(), pE.data(), pT.data(), nullptr, 0, s));
+                                      pev.data(), pE.data(), pT.data(),
+                                      *precision == RIMP2_PREC_SPLIT ? nullptr : zeros.data(), 0,
+                                      s));
     int rc = rimp2_batch_plan_execute(plan, s);
     rimp2_batch_plan_destroy(plan);
     RIMP2_TRY(rc);
-  } else {
-    for (int f = 0; f < nf; ++f) {
-      PlainEnergyArgs a;
-      a.Ca = pc[f];
-      a.NBA = NBA[f];
-      a.nvirt = nvirt[f];
-      a.nocc = nocc[f];
-      a.eo = peo[f];
-      a.ev = pev[f];
-      a.Epair = pE[f];
-      a.Etot = pT[f];
-      a.tamp = nullptr;
-      a.pairs = nullptr;
-      a.npairs = 0;
-      RIMP2_TRY(plain_energy_f64(a, s));
-    }
   }
   oe = 0;
   for (int f = 0; f < nf; ++f) {

@@ -103,6 +103,20 @@ int probe_fp64_peak(double *tflops, cudaStream_t s);
 void plain_energy_scratch_sizes(int nvirt, int nocc, long long *npairs, long long *nitems);
 int plain_energy_f64_scratch(const PlainEnergyArgs &a, int *pairs_scratch, double *part_scratch,
                              cudaStream_t s);
+// Batched plain FP64 energies: every fragment's (pair, 64x64 tile pair) items
+// in one persistent launch, then per-fragment compensated reductions.
+struct PlainFrag {
+  const double *Ca, *eo, *ev;
+  double *Epair, *Etot;
+  int nocc, nvirt, NBA, ntp;
+  int pair_base;        // first global pair index
+  long long item_base;  // first work item
+};
+struct PlainPlan;
+int plain_plan_create(PlainPlan **out, int nfrag, const PlainFrag *frags, cudaStream_t s);
+int plain_plan_record(PlainPlan *P, cudaStream_t s);  // no sync, no allocation
+int plain_plan_launches(const PlainPlan *P);
+void plain_plan_destroy(PlainPlan *P);
 
 // ---- split-precision tcgen05 path (split_kernels.cu) ---------------------------
 struct SplitEnergyArgs {

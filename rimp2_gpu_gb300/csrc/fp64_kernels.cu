@@ -17,6 +17,9 @@
 // the CTA count is large enough to fill all 152 SMs several times.
 #include "common.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace rimp2 {
 
 namespace {
@@ -146,22 +149,14 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// part[item] = contribution of tile pair (A,B) to e_ij of pair p
-__global__ void __launch_bounds__(NTHR) plain_energy_kernel(const double *__restrict__ Ca, int NBA,
-                                                            int nvirt, int nocc,
-                                                            const double *__restrict__ eo,
-                                                            const double *__restrict__ ev,
-                                                            const int *__restrict__ pairs,
-                                                            int ntile, double *__restrict__ part,
-                                                            double *__restrict__ tamp) {
-  __shared__ double P[4][TM][KP];  // C_iA, C_jB, C_jA, C_iB slabs
-  __shared__ double red[NTHR / 32];
-  const int ntp = ntile * (ntile + 1) / 2;
-  const long long item = blockIdx.x;
-  const int p = (int)(item / ntp), q = (int)(item % ntp);
-  int tA, tB;
-  decode_tri(q, tA, tB);
-  const int i = pairs[2 * p], j = pairs[2 * p + 1];
+// Energy contribution of tile pair (tA,tB) of occupied pair (i<=j); the
+// block sum is valid in thread 0.  Shared staging P and red are the caller's.
+__device__ __forceinline__ double plain_tile_pair(double (&P)[4][TM][KP], double *red,
+                                                  const double *__restrict__ Ca, int NBA,
+                                                  int nvirt, int nocc,
+                                                  const double *__restrict__ eo,
+                                                  const double *__restrict__ ev, int i, int j,
+                                                  int tA, int tB, double *__restrict__ tamp) {
   const bool same = (i == j);
   const int a0 = tA * TM, b0 = tB * TN;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -254,10 +249,74 @@ __global__ void __launch_bounds__(NTHR) plain_energy_kernel(const double *__rest
   e = warp_sum(e);
   if (lane == 0) red[warp] = e;
   __syncthreads();
-  if (tid == 0) {
-    double s = 0.0;
+  double s = 0.0;
+  if (tid == 0)
     for (int w = 0; w < NTHR / 32; ++w) s += red[w];
-    part[item] = s;
+  return s;
+}
+
+// part[item] = contribution of tile pair (A,B) to e_ij of pair p
+__global__ void __launch_bounds__(NTHR, 2) plain_energy_kernel(const double *__restrict__ Ca, int NBA,
+                                                            int nvirt, int nocc,
+                                                            const double *__restrict__ eo,
+                                                            const double *__restrict__ ev,
+                                                            const int *__restrict__ pairs,
+                                                            int ntile, double *__restrict__ part,
+                                                            double *__restrict__ tamp) {
+  __shared__ double P[4][TM][KP];  // C_iA, C_jB, C_jA, C_iB slabs
+  __shared__ double red[NTHR / 32];
+  const int ntp = ntile * (ntile + 1) / 2;
+  const long long item = blockIdx.x;
+  const int p = (int)(item / ntp), q = (int)(item % ntp);
+  int tA, tB;
+  decode_tri(q, tA, tB);
+  const double s = plain_tile_pair(P, red, Ca, NBA, nvirt, nocc, eo, ev, pairs[2 * p],
+                                   pairs[2 * p + 1], tA, tB, tamp);
+  if (threadIdx.x == 0) part[item] = s;
+}
+
+// Batched form: one persistent launch drains a queue of (fragment, pair,
+// tile pair) items over every fragment of the batch.  Fragments are ordered
+// heaviest first (by NBA, the K length of each item), so the long items lead
+// the queue and the short ones fill the tail.
+__device__ __forceinline__ void decode_pair_ij(int p, int &i, int &j) {
+  // p = j*(j+1)/2 + i, 0 <= i <= j
+  int jj = (int)((sqrt(8.0 * p + 1.0) - 1.0) * 0.5);
+  while ((jj + 1) * (jj + 2) / 2 <= p) ++jj;
+  while (jj * (jj + 1) / 2 > p) --jj;
+  j = jj;
+  i = p - jj * (jj + 1) / 2;
+}
+
+__global__ void __launch_bounds__(NTHR) plain_batch_kernel(const PlainFrag *__restrict__ fr,
+                                                           int nfrag, long long nitems,
+                                                           unsigned int *queue,
+                                                           double *__restrict__ part) {
+  __shared__ double P[4][TM][KP];
+  __shared__ double red[NTHR / 32];
+  __shared__ long long s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (long long)atomicAdd(queue, 1u);
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= nitems) break;
+    int lo = 0, hi = nfrag - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (fr[mid].item_base <= item)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const PlainFrag &F = fr[lo];
+    const long long loc = item - F.item_base;
+    int i, j, tA, tB;
+    decode_pair_ij((int)(loc / F.ntp), i, j);
+    decode_tri((int)(loc % F.ntp), tA, tB);
+    const double s = plain_tile_pair(P, red, F.Ca, F.NBA, F.nvirt, F.nocc, F.eo, F.ev, i, j, tA,
+                                     tB, nullptr);
+    if (threadIdx.x == 0) part[item] = s;
+    __syncthreads();  // s_item and red are rewritten by the next item
   }
 }
 
@@ -308,8 +367,8 @@ __global__ void pair_reduce_kernel(const double *__restrict__ part, int nper, co
   }
 }
 
-// Etot = sum_ij Epair(i,j): one block of 1024 threads, compensated tree
-__global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot) {
+// Etot = sum_ij Epair(i,j): one block, compensated tree
+__device__ __forceinline__ void total_reduce_body(const double *Epair, int nocc, double *Etot) {
   __shared__ double ss[32], sc[32];
   double s = 0.0, c = 0.0;
   const size_t n = (size_t)nocc * nocc;
@@ -335,6 +394,10 @@ __global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot)
   }
 }
 
+__global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot) {
+  total_reduce_body(Epair, nocc, Etot);
+}
+
 __global__ void make_pairs_kernel(int nocc, int *pairs) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   const int np = nocc * (nocc + 1) / 2;
@@ -344,6 +407,46 @@ __global__ void make_pairs_kernel(int nocc, int *pairs) {
   while (j * (j + 1) / 2 > n) --j;
   pairs[2 * n] = n - j * (j + 1) / 2;
   pairs[2 * n + 1] = j;
+}
+
+// one warp per (fragment, pair) of a plain batch
+__global__ void pair_reduce_plain_batch_kernel(const PlainFrag *__restrict__ fr, int nfrag,
+                                               int npairs_total, const double *__restrict__ part) {
+  const int gp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gp >= npairs_total) return;
+  int lo = 0, hi = nfrag - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (fr[mid].pair_base <= gp)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const PlainFrag &F = fr[lo];
+  const int p = gp - F.pair_base;
+  const double *src = part + F.item_base + (long long)p * F.ntp;
+  double s = 0.0, c = 0.0;
+  for (int r = lane; r < F.ntp; r += 32) {
+    double t, e;
+    two_sum(s, src[r], t, e);
+    s = t;
+    c += e;
+  }
+  warp_sum_comp(s, c);
+  if (lane == 0) {
+    int i, j;
+    decode_pair_ij(p, i, j);
+    const double v = s + c;
+    F.Epair[i + (size_t)F.nocc * j] = v;
+    F.Epair[j + (size_t)F.nocc * i] = v;
+  }
+}
+
+// one block per fragment of a plain batch: Etot_f = sum_ij Epair_f(i,j)
+__global__ void total_reduce_plain_batch_kernel(const PlainFrag *__restrict__ fr) {
+  const PlainFrag &F = fr[blockIdx.x];
+  total_reduce_body(F.Epair, F.nocc, F.Etot);
 }
 
 void count_launch(int n);
@@ -479,5 +582,88 @@ int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s) {
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;
 }
+
+
+// A planned plain FP64 batch: fragment table, per-item partials, queue.
+struct PlainPlan {
+  int nfrag = 0, npairs_total = 0, grid = 0;
+  long long nitems = 0;
+  DevBuf frags, part, queue;
+};
+
+int plain_plan_create(PlainPlan **out, int nfrag, const PlainFrag *in, cudaStream_t s) {
+  *out = nullptr;
+  std::vector<PlainFrag> fh(in, in + nfrag);
+  // heaviest items (longest K) first in the queue
+  std::stable_sort(fh.begin(), fh.end(),
+                   [](const PlainFrag &x, const PlainFrag &y) { return x.NBA > y.NBA; });
+  long long item = 0;
+  int pb = 0;
+  for (auto &F : fh) {
+    const int nt = (F.nvirt + TM - 1) / TM;
+    F.ntp = nt * (nt + 1) / 2;
+    F.pair_base = pb;
+    F.item_base = item;
+    const int np = F.nocc * (F.nocc + 1) / 2;
+    pb += np;
+    item += (long long)np * F.ntp;
+  }
+  if (item >= 2147483647LL) {
+    set_error("plain batch too large for one launch (%lld items)", item);
+    return RIMP2_ERR_ARG;
+  }
+  PlainPlan *P = new PlainPlan();
+  P->nfrag = nfrag;
+  P->npairs_total = pb;
+  P->nitems = item;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, plain_batch_kernel, NTHR, 0);
+  if (e != cudaSuccess || occ < 1) occ = 1;
+  P->grid = (int)std::min<long long>(item > 0 ? item : 1, (long long)nsm * occ);
+  int rc = P->frags.alloc(sizeof(PlainFrag) * (size_t)nfrag, s);
+  if (rc == RIMP2_OK) rc = P->part.alloc(sizeof(double) * (size_t)std::max<long long>(item, 1), s);
+  if (rc == RIMP2_OK) rc = P->queue.alloc(sizeof(unsigned int), s);
+  if (rc == RIMP2_OK &&
+      cudaMemcpyAsync(P->frags.p, fh.data(), sizeof(PlainFrag) * (size_t)nfrag,
+                      cudaMemcpyHostToDevice, s) != cudaSuccess) {
+    set_error("plain batch descriptor copy failed");
+    rc = RIMP2_ERR_CUDA;
+  }
+  // the descriptor copy reads fh: finish it before fh goes out of scope
+  if (rc == RIMP2_OK && cudaStreamSynchronize(s) != cudaSuccess) {
+    set_error("plain batch descriptor copy failed");
+    rc = RIMP2_ERR_CUDA;
+  }
+  if (rc != RIMP2_OK) {
+    delete P;
+    return rc;
+  }
+  *out = P;
+  return RIMP2_OK;
+}
+
+int plain_plan_launches(const PlainPlan *P) { return P && P->nfrag ? 3 : 0; }
+
+int plain_plan_record(PlainPlan *P, cudaStream_t s) {
+  if (!P || P->nfrag == 0) return RIMP2_OK;
+  if (inject_fault("launch")) {
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  const PlainFrag *fr = P->frags.as<PlainFrag>();
+  RIMP2_CK(cudaMemsetAsync(P->queue.p, 0, sizeof(unsigned int), s));
+  plain_batch_kernel<<<P->grid, NTHR, 0, s>>>(fr, P->nfrag, P->nitems, P->queue.as<unsigned int>(),
+                                              P->part.as<double>());
+  pair_reduce_plain_batch_kernel<<<(unsigned)((P->npairs_total + 7) / 8), 256, 0, s>>>(
+      fr, P->nfrag, P->npairs_total, P->part.as<double>());
+  total_reduce_plain_batch_kernel<<<P->nfrag, 1024, 0, s>>>(fr);
+  count_launch(3);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+void plain_plan_destroy(PlainPlan *P) { delete P; }
 
 }  // namespace rimp2

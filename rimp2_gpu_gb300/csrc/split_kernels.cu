@@ -1246,12 +1246,20 @@ __global__ void ao_slice_kernel(const double *__restrict__ ao, int NBA, int nbas
 // an instantiated CUDA graph of the whole evaluation.
 struct SplitPlan {
   Group g[2];
+  PlainPlan *plain = nullptr;  // fragments planned in plain FP64 (slice count 0)
   int nsm = 0;
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
   ~SplitPlan() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
+    plain_plan_destroy(plain);
+  }
+  int launches() const {
+    int n = plain_plan_launches(plain);
+    for (auto &x : g)
+      if (x.nfrag) n += 5;
+    return n;
   }
 };
 
@@ -1268,7 +1276,22 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
   cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, dev);
   P->g[0].nsl = 2;
   P->g[1].nsl = 3;
+  std::vector<PlainFrag> plain;
   for (int f = 0; f < nfrag; ++f) {
+    if (nslices && nslices[f] == 0) {
+      PlainFrag F;
+      memset(&F, 0, sizeof F);
+      F.Ca = Ca[f];
+      F.eo = eo[f];
+      F.ev = ev[f];
+      F.Epair = Epair[f];
+      F.Etot = Etot[f];
+      F.nocc = nocc[f];
+      F.nvirt = nvirt[f];
+      F.NBA = NBA[f];
+      plain.push_back(F);
+      continue;
+    }
     FragDesc F;
     memset(&F, 0, sizeof F);
     F.nocc = nocc[f];
@@ -1290,6 +1313,13 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
       return rc;
     }
   }
+  if (!plain.empty()) {
+    int rc = plain_plan_create(&P->plain, (int)plain.size(), plain.data(), s);
+    if (rc != RIMP2_OK) {
+      delete P;
+      return rc;
+    }
+  }
   if (graph) {
     // the captured sequence needs the workspace already in place
     cudaError_t e = cudaStreamSynchronize(s);
@@ -1299,10 +1329,13 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
       delete P;
       return RIMP2_ERR_CUDA;
     }
-    int rc = RIMP2_OK;
+    const long long n0 = rimp2_kernel_launch_count();
+    int rc = plain_plan_record(P->plain, s);
     for (auto &g : P->g)
       if (rc == RIMP2_OK) rc = record_group(g, s, P->nsm, nullptr);
     e = cudaStreamEndCapture(s, &P->graph);
+    // captured launches run at each graph launch, not here
+    count_launch(-(int)(rimp2_kernel_launch_count() - n0));
     if (rc != RIMP2_OK || e != cudaSuccess) {
       if (rc == RIMP2_OK) set_error("graph capture failed: %s", cudaGetErrorString(e));
       delete P;
@@ -1322,13 +1355,21 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
 int split_plan_execute(SplitPlan *P, cudaStream_t s) {
   if (P->gexec) {
     RIMP2_CK(cudaGraphLaunch(P->gexec, s));
-    count_launch(7);
+    count_launch(P->launches());
     return RIMP2_OK;
   }
   const bool timed = timing_enabled();
   cudaEvent_t ev[4];
   if (timed)
     for (int k = 0; k < 4; ++k) RIMP2_CK(cudaEventCreate(&ev[k]));
+  // a plan of plain fragments only is timed as one kernel interval
+  const bool plain_only = !P->g[0].nfrag && !P->g[1].nfrag;
+  if (timed && plain_only) {
+    RIMP2_CK(cudaEventRecord(ev[0], s));
+    RIMP2_CK(cudaEventRecord(ev[1], s));
+  }
+  RIMP2_TRY(plain_plan_record(P->plain, s));
+  if (timed && plain_only) RIMP2_CK(cudaEventRecord(ev[2], s));
   for (auto &g : P->g) RIMP2_TRY(record_group(g, s, P->nsm, timed ? ev : nullptr));
   if (timed) {
     RIMP2_CK(cudaEventRecord(ev[3], s));

@@ -34,7 +34,11 @@ def test_energy_batched_host_api(frags, prec, tol):
         assert abs(E - f[4]) <= tol * abs(f[4])
 
 
-def test_batch_plan_graph_replay(frags):
+@pytest.mark.parametrize("nslices", [None, [0, 1, 2, 0, 1, 0], [0] * len(SHAPES)],
+                         ids=["buckets", "mixed", "fp64"])
+def test_batch_plan_graph_replay(frags, nslices):
+    """Slice count 0 puts a fragment in the plain FP64 persistent launch: its
+    energies must meet the FP64 bar (1e-11), the split ones 1e-7."""
     import torch
     from rimp2_gpu_gb300 import api
     dev = []
@@ -48,14 +52,19 @@ def test_batch_plan_graph_replay(frags):
     desc = [(n, v, b, t["C"].data_ptr(), t["eo"].data_ptr(), t["ev"].data_ptr(), t["E"].data_ptr(),
              t["T"].data_ptr()) for n, v, b, t in dev]
     st = torch.cuda.Stream()
-    plan = api.BatchPlan(desc, graph=True, stream=st.cuda_stream)
+    plan = api.BatchPlan(desc, nslices=nslices, graph=True, stream=st.cuda_stream)
     results = []
+    ns = nslices or [1] * len(SHAPES)
+    expect_launches = sum(3 if k == 0 else 5 for k in set(ns))
     for rep in range(3):
         for _, _, _, t in dev:
             t["E"].zero_()
             t["T"].zero_()
         torch.cuda.synchronize()
+        n0 = api.kernel_launch_count()
         plan.execute(stream=st.cuda_stream)
+        if nslices is not None:
+            assert api.kernel_launch_count() - n0 == expect_launches
         st.synchronize()
         api.sync_status(st.cuda_stream)
         results.append([(t["E"].cpu().numpy().copy(), t["T"].item()) for _, _, _, t in dev])
@@ -64,10 +73,11 @@ def test_batch_plan_graph_replay(frags):
         for (Ea, Ta), (Eb, Tb) in zip(results[0], results[rep]):
             np.testing.assert_array_equal(Ea, Eb)
             assert Ta == Tb
-    for (Ep, E), f, (n, _, _, _) in zip(results[0], frags, dev):
+    for (Ep, E), f, (n, _, _, _), k in zip(results[0], frags, dev, ns):
+        tol = 1e-11 if k == 0 else 1e-7
         Ep = Ep.reshape(n, n, order="F")
-        assert (np.abs(Ep - f[3]) / np.abs(f[3])).max() <= 1e-7
-        assert abs(E - f[4]) <= 1e-7 * abs(f[4])
+        assert (np.abs(Ep - f[3]) / np.abs(f[3])).max() <= tol
+        assert abs(E - f[4]) <= tol * abs(f[4])
 
 
 def test_bucket_table_roundtrip():
