@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--ao-transform", choices=["split", "fp64"], default="split",
                     help="AO->MO transform on the tensor cores (split) or in FP64; the metric "
                          "Cholesky and the triangular solve are FP64 either way")
+    ap.add_argument("--ao-nbas", type=int, default=None,
+                    help="AO pipeline: every fragment with this nbas (profiling small cases)")
     ap.add_argument("--nocc", type=int, default=None, help="override (profiling small cases)")
     ap.add_argument("--nvirt", type=int, default=None)
     ap.add_argument("--nba", type=int, default=None)
@@ -662,6 +664,9 @@ def run_ao(args):
     st = torch.cuda.Stream(device=dev)
     sp = st.cuda_stream
     shapes = ao_shapes(args.ao_fragments)
+    if args.ao_nbas:
+        b = args.ao_nbas
+        shapes = [(b, 3 * b, b // 10, b - b // 10)] * len(shapes)
     maxao = max(b * b * nba for b, nba, _, _ in shapes)
     maxv = max(nba * nba for _, nba, _, _ in shapes)
     maxb = max(nba * nvirt * nocc for _, nba, nocc, nvirt in shapes)
@@ -767,8 +772,9 @@ def run_ao(args):
                       if args.ao_transform == "split" else
                       "f64 front end; f16 Ozaki slices / f32 tensor accumulation for the energy"),
             "data": "synthetic (device Philox AO integrals and metric, numpy QR MO coefficients)",
-            "config": {"workload": f"pipeline from AO integrals, {len(shapes)} fragments "
-                                   "(nbas U[128,768], NBA=3 nbas, nocc=nbas/10)",
+            "config": {"workload": f"pipeline from AO integrals, {len(shapes)} fragments " + (
+                           "(nbas U[128,768], NBA=3 nbas, nocc=nbas/10)" if not args.ao_nbas else
+                           f"(nbas={args.ao_nbas}, NBA=3 nbas, nocc=nbas/10; reduced case)"),
                        "ao_transform": args.ao_transform,
                        "front_end_ms": fe_m, "energy_ms": en_m,
                        "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,

@@ -85,6 +85,7 @@ struct GemmDesc {
   // from the two batch indices (used by the toccA/tvirtA g/D step)
   const double *eo, *ev;
   int denom;  // 0 none, 1 batch=(i,j) row=a col=b
+  int lower;  // 1: only output tiles touching the lower triangle (m >= n) are computed
 };
 int launch_gemm_f64(const GemmDesc &g, cudaStream_t s);
 

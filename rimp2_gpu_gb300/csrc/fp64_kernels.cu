@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(NTHR) gemm_f64_kernel(GemmDesc g) {
     double *Cb = g.C + b0 * g.sCb0 + b1 * g.sCb1;
     for (int by = blockIdx.y; by * TN < g.N; by += gridDim.y) {
       const int m0 = blockIdx.x * TM, n0 = by * TN;
+      if (g.lower && n0 > m0 + TM - 1) continue;  // tile strictly above the diagonal
       double acc[4][2][2];
 #pragma unroll
       for (int x = 0; x < 4; ++x)

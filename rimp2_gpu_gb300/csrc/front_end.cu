@@ -8,10 +8,11 @@
 // counterpart there.  Every product runs on the FP64 DMMA GEMM of
 // fp64_kernels.cu; the Cholesky and the solve are blocked (64) so that all
 // but O(n*64^2) of their work is GEMM:
-//   Cholesky: diagonal-block factorisation (one CTA), panel solve, trailing
-//             update C -= P P^T;
-//   solve:    X_k = inv(L_kk) B_k (explicit 64x64 inverse, GEMM), then
-//             B_rest -= L_rest,k X_k.
+//   Cholesky: diagonal-block factorisation and inverse (one CTA), panel
+//             P L_kk^{-T} (GEMM), trailing update C -= P P^T on the
+//             lower-triangle tiles;
+//   solve:    all diagonal-block inverses in one launch, then
+//             X_k = inv(L_kk) B_k and B_rest -= L_rest,k X_k (GEMMs).
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -34,118 +35,181 @@ GemmDesc gdesc() {
   return g;
 }
 
-// in-place Cholesky of the b x b diagonal block at (k0,k0) of V (ld n);
-// sets *bad = k+1 on a non-positive pivot
-__global__ void potrf_block_kernel(double *V, int n, int k0, int b, int *bad) {
-  __shared__ double A[NB][NB + 1];
-  for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
-    const int r = t % b, c = t / b;
-    A[r][c] = V[(size_t)(k0 + r) + (size_t)n * (k0 + c)];
+// Diagonal 64x64 blocks: factorisation and triangular inverse in shared
+// memory, 256 threads.  Blocks narrower than 64 (the last one) are padded
+// with the identity, so the same code runs on every block.
+constexpr int DP = NB + 1;                        // padded row (doubles)
+constexpr int DIAG_SMEM = (2 * NB * DP + 5 * NB + 1) * sizeof(double);
+
+__device__ __forceinline__ void load_block(double (*A)[DP], const double *V, int n, int k0, int b) {
+  for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+    const int r = t & (NB - 1), c = t >> 6;
+    A[r][c] = (r < b && c < b) ? V[(size_t)(k0 + r) + (size_t)n * (k0 + c)] : (r == c ? 1.0 : 0.0);
   }
   __syncthreads();
-  for (int k = 0; k < b; ++k) {
+}
+
+// X = A^{-1} for lower-triangular A (both NB x NB in shared memory): row by
+// row forward substitution, four threads per column sharing each dot product.
+// FP64 arithmetic is scarce on this part, so divisions become one
+// reciprocal per row (rdiag, NB doubles of shared memory).
+__device__ void tri_inverse(double (*A)[DP], double (*X)[DP], double *part, double *rdiag) {
+  const int c = threadIdx.x & (NB - 1), q = threadIdx.x >> 6;  // q = 0..3
+  if (threadIdx.x < NB) rdiag[threadIdx.x] = 1.0 / A[threadIdx.x][threadIdx.x];
+  __syncthreads();
+  for (int r = 0; r < NB; ++r) {
+    double s = 0.0;
+    for (int p = c + q; p < r; p += 4) s += A[r][p] * X[p][c];
+    part[q * NB + c] = s;
+    __syncthreads();
+    if (q == 0) {
+      const double d = (r == c ? 1.0 : 0.0) - (part[c] + part[NB + c] + part[2 * NB + c] +
+                                               part[3 * NB + c]);
+      X[r][c] = (c <= r) ? d * rdiag[r] : 0.0;
+    }
+    __syncthreads();
+  }
+}
+
+// In-place Cholesky of the b x b diagonal block at (k0,k0) of V (ld n) and
+// its inverse into Linv (NB x NB, column-major); *bad = pivot+1 on a
+// non-positive pivot.
+__global__ void __launch_bounds__(256) potrf_inv_block_kernel(double *V, int n, int k0, int b,
+                                                             double *Linv, int *bad) {
+  extern __shared__ double dsm[];
+  double(*A)[DP] = reinterpret_cast<double(*)[DP]>(dsm);
+  double(*X)[DP] = reinterpret_cast<double(*)[DP]>(dsm + NB * DP);
+  double *part = dsm + 2 * NB * DP;
+  double *rdiag = part + 4 * NB;
+  double *rpiv = rdiag + NB;
+  load_block(A, V, n, k0, b);
+  const int c = threadIdx.x & (NB - 1), r0 = threadIdx.x >> 6;
+  for (int k = 0; k < NB; ++k) {
     if (threadIdx.x == 0) {
       const double d = A[k][k];
-      if (!(d > 0.0)) {
+      double l = 1.0;
+      if (!(d > 0.0))
         atomicCAS(bad, 0, k0 + k + 1);
-        A[k][k] = 1.0;
-      } else {
-        A[k][k] = sqrt(d);
-      }
+      else
+        l = sqrt(d);
+      A[k][k] = l;
+      *rpiv = 1.0 / l;
     }
     __syncthreads();
-    const double dk = A[k][k];
-    for (int r = k + 1 + threadIdx.x; r < b; r += blockDim.x) A[r][k] /= dk;
+    if (threadIdx.x > k && threadIdx.x < NB) A[threadIdx.x][k] *= *rpiv;
     __syncthreads();
-    // rank-1 update of the remaining lower triangle
-    for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
-      const int r = t % b, c = t / b;
-      if (c > k && r >= c) A[r][c] -= A[r][k] * A[c][k];
+    // trailing lower triangle: column c, rows r >= c with r = r0 (mod 4)
+    if (c > k) {
+      const double ck = A[c][k];
+      for (int r = c + ((r0 - c) & 3); r < NB; r += 4) A[r][c] -= A[r][k] * ck;
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
-    const int r = t % b, c = t / b;
-    V[(size_t)(k0 + r) + (size_t)n * (k0 + c)] = (r >= c) ? A[r][c] : 0.0;
+  tri_inverse(A, X, part, rdiag);
+  for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+    const int r = t & (NB - 1), cc = t >> 6;
+    if (r < b && cc < b) V[(size_t)(k0 + r) + (size_t)n * (k0 + cc)] = (r >= cc) ? A[r][cc] : 0.0;
+    Linv[t] = X[r][cc];
   }
 }
 
-// rows below the diagonal block: P := P L_kk^{-T}  (one thread per row)
-__global__ void panel_solve_kernel(double *V, int n, int k0, int b) {
-  __shared__ double L[NB][NB + 1];
-  for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
-    const int r = t % b, c = t / b;
-    L[r][c] = V[(size_t)(k0 + r) + (size_t)n * (k0 + c)];
+// Inverses of every diagonal block of the lower-triangular L (one CTA per
+// block) into Linv (nblk x NB x NB).
+__global__ void __launch_bounds__(256) tri_inverse_blocks_kernel(const double *L, int n,
+                                                                double *Linv) {
+  extern __shared__ double dsm[];
+  double(*A)[DP] = reinterpret_cast<double(*)[DP]>(dsm);
+  double(*X)[DP] = reinterpret_cast<double(*)[DP]>(dsm + NB * DP);
+  double *part = dsm + 2 * NB * DP;
+  double *rdiag = part + 4 * NB;
+  const int k0 = blockIdx.x * NB;
+  const int b = n - k0 < NB ? n - k0 : NB;
+  load_block(A, L, n, k0, b);
+  // only the lower triangle of L is meaningful
+  for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+    const int r = t & (NB - 1), c = t >> 6;
+    if (r < c) A[r][c] = 0.0;
   }
   __syncthreads();
-  const int row = k0 + b + blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= n) return;
-  double x[NB];
-  for (int c = 0; c < b; ++c) {
-    double s = V[(size_t)row + (size_t)n * (k0 + c)];
-    for (int p = 0; p < c; ++p) s -= x[p] * L[c][p];
-    x[c] = s / L[c][c];
-  }
-  for (int c = 0; c < b; ++c) V[(size_t)row + (size_t)n * (k0 + c)] = x[c];
+  tri_inverse(A, X, part, rdiag);
+  double *out = Linv + (size_t)blockIdx.x * NB * NB;
+  for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) out[t] = X[t & (NB - 1)][t >> 6];
 }
 
-// inverse of the lower-triangular b x b block at (k0,k0) of L (ld n) into
-// Linv (b x b, ld NB): one thread per column, forward substitution
-__global__ void trinv_block_kernel(const double *L, int n, int k0, int b, double *Linv) {
-  __shared__ double A[NB][NB + 1];
-  for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
-    const int r = t % b, c = t / b;
-    A[r][c] = L[(size_t)(k0 + r) + (size_t)n * (k0 + c)];
+// The shared-memory opt-in is per device: set it on the current device.
+int diag_kernels_init() {
+  const bool ok =
+      cudaFuncSetAttribute(potrf_inv_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           DIAG_SMEM) == cudaSuccess &&
+      cudaFuncSetAttribute(tri_inverse_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           DIAG_SMEM) == cudaSuccess;
+  if (!ok) {
+    set_error("diagonal-block kernels: shared-memory attribute failed");
+    return RIMP2_ERR_CUDA;
   }
-  __syncthreads();
-  const int c = threadIdx.x;
-  if (c >= NB) return;
-  double x[NB];
-  for (int r = 0; r < NB; ++r) {
-    double v = 0.0;
-    if (c < b && r < b && r >= c) {
-      double s = (r == c) ? 1.0 : 0.0;
-      for (int p = c; p < r; ++p) s -= A[r][p] * x[p];
-      v = s / A[r][r];
-    }
-    x[r] = v;
-  }
-  for (int r = 0; r < NB; ++r) Linv[r + NB * c] = x[r];
+  return RIMP2_OK;
 }
 
 }  // namespace
 
 // V (n x n, ld n, device) -> lower Cholesky factor in place (strict upper
 // zeroed block by block).  Returns RIMP2_ERR_ARG if V is not positive definite.
+// Per 64-column block k: factor and invert the diagonal block (one CTA),
+// panel P := P L_kk^{-T} as a GEMM with the inverse (into a work panel), the
+// trailing update C -= P P^T on the lower-triangle tiles, and the panel
+// copied back into V.
 int dev_cholesky(int n, double *V, cudaStream_t s) {
-  DevBuf bad;
+  RIMP2_TRY(diag_kernels_init());
+  DevBuf bad, inv, panel;
   RIMP2_TRY(bad.alloc(sizeof(int), s));
+  RIMP2_TRY(inv.alloc(sizeof(double) * NB * NB, s));
+  RIMP2_TRY(panel.alloc(sizeof(double) * (size_t)(n > NB ? n - NB : 1) * NB, s));
   RIMP2_CK(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int b = n - k0 < NB ? n - k0 : NB;
-    potrf_block_kernel<<<1, 256, 0, s>>>(V, n, k0, b, bad.as<int>());
+    potrf_inv_block_kernel<<<1, 256, DIAG_SMEM, s>>>(V, n, k0, b, inv.as<double>(),
+                                                     bad.as<int>());
     count_launch(1);
     const int rest = n - k0 - b;
     if (rest > 0) {
-      panel_solve_kernel<<<(rest + 127) / 128, 128, 0, s>>>(V, n, k0, b);
-      count_launch(1);
-      // trailing update C -= P P^T on the whole trailing square
-      GemmDesc g = gdesc();
-      g.M = rest;
-      g.N = rest;
-      g.K = b;
-      g.alpha = -1.0;
-      g.beta = 1.0;
-      g.A = V + (size_t)(k0 + b) + (size_t)n * k0;
-      g.sAm = 1;
-      g.sAk = n;
-      g.B = g.A;
-      g.sBk = n;
-      g.sBn = 1;
-      g.C = V + (size_t)(k0 + b) + (size_t)n * (k0 + b);
-      g.sCm = 1;
-      g.sCn = n;
-      RIMP2_TRY(launch_gemm_f64(g, s));
+      double *Pv = V + (size_t)(k0 + b) + (size_t)n * k0;
+      {  // panel(rest x b) = P Linv^T
+        GemmDesc g = gdesc();
+        g.M = rest;
+        g.N = b;
+        g.K = b;
+        g.A = Pv;
+        g.sAm = 1;
+        g.sAk = n;
+        g.B = inv.as<double>();
+        g.sBk = NB;
+        g.sBn = 1;
+        g.C = panel.as<double>();
+        g.sCm = 1;
+        g.sCn = rest;
+        RIMP2_TRY(launch_gemm_f64(g, s));
+      }
+      {  // trailing update C -= panel panel^T (lower-triangle tiles)
+        GemmDesc g = gdesc();
+        g.M = rest;
+        g.N = rest;
+        g.K = b;
+        g.alpha = -1.0;
+        g.beta = 1.0;
+        g.lower = 1;
+        g.A = panel.as<double>();
+        g.sAm = 1;
+        g.sAk = rest;
+        g.B = panel.as<double>();
+        g.sBk = rest;
+        g.sBn = 1;
+        g.C = V + (size_t)(k0 + b) + (size_t)n * (k0 + b);
+        g.sCm = 1;
+        g.sCn = n;
+        RIMP2_TRY(launch_gemm_f64(g, s));
+      }
+      RIMP2_CK(cudaMemcpy2DAsync(Pv, sizeof(double) * n, panel.p, sizeof(double) * rest,
+                                 sizeof(double) * rest, b, cudaMemcpyDeviceToDevice, s));
     }
     // zero the strict upper part of this block column above the block
     if (k0 > 0) RIMP2_CK(cudaMemset2DAsync(V + (size_t)n * k0, sizeof(double) * n, 0,
@@ -163,19 +227,24 @@ int dev_cholesky(int n, double *V, cudaStream_t s) {
 }
 
 // X = L^{-1} B for B (n x m, ld n).  B is overwritten (used as workspace).
+// The inverses of all diagonal blocks come from one launch; then per block
+// X_k = inv(L_kk) B_k and B_rest -= L_rest,k X_k (both GEMMs).
 int dev_trsm_lower(int n, int m, const double *L, double *B, double *X, cudaStream_t s) {
+  RIMP2_TRY(diag_kernels_init());
+  const int nblk = (n + NB - 1) / NB;
   DevBuf inv;
-  RIMP2_TRY(inv.alloc(sizeof(double) * NB * NB, s));
+  RIMP2_TRY(inv.alloc(sizeof(double) * NB * NB * (size_t)nblk, s));
+  tri_inverse_blocks_kernel<<<nblk, 256, DIAG_SMEM, s>>>(L, n, inv.as<double>());
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
   for (int k0 = 0; k0 < n; k0 += NB) {
     const int b = n - k0 < NB ? n - k0 : NB;
-    trinv_block_kernel<<<1, NB, 0, s>>>(L, n, k0, b, inv.as<double>());
-    count_launch(1);
     {  // X_k = inv(L_kk) B_k
       GemmDesc g = gdesc();
       g.M = b;
       g.N = m;
       g.K = b;
-      g.A = inv.as<double>();
+      g.A = inv.as<double>() + (size_t)(k0 / NB) * NB * NB;
       g.sAm = 1;
       g.sAk = NB;
       g.B = B + k0;

@@ -1163,81 +1163,117 @@ __global__ void __launch_bounds__(192, 1)
   }
 }
 
-// AO tensor rows: row m' = mu + nbas*alpha of (alpha|mu nu) over K = nu, one
-// thread per row, threads ordered alpha-fastest so that every load of a
-// nu-step is coalesced.  Same scale rule and slice layout as slice_batch_kernel.
-__global__ void ao_slice_kernel(const double *__restrict__ ao, int NBA, int nbas, long long nrows_pad,
-                                int nks, int nsl, long long plane, __half *__restrict__ slices,
-                                float *__restrict__ inv_scale) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// AO tensor rows: row m' = mu + nbas*alpha of (alpha|mu nu) over K = nu.
+// One CTA owns 32 alpha x 8 mu rows, one thread per row, warps alpha-fastest
+// so every load of a nu-step is one 256-byte segment.  Same scale rule and
+// slice layout as slice_batch_kernel.  The FP16 slices of each 64-wide nu
+// chunk are staged in shared memory (16-byte chunks XOR-swizzled by alpha)
+// and written out row-contiguous: the 8 mu rows of one alpha are 1 KB of
+// consecutive memory.  The first CTA also sets the scale of the padding rows
+// (their slices are zeroed by the host).
+constexpr int AO_TA = 32, AO_TM = 8, AO_ROWS = AO_TA * AO_TM;
+
+__global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restrict__ ao, int NBA,
+                                                          int nbas, long long nrows_pad, int nks,
+                                                          int nsl, long long plane,
+                                                          __half *__restrict__ slices,
+                                                          float *__restrict__ inv_scale) {
+  extern __shared__ uint4 stage[];  // [nsl][AO_ROWS rows][8 chunks of 8 halves]
+  const int a_l = threadIdx.x & (AO_TA - 1), m_l = threadIdx.x / AO_TA;
+  const int al = blockIdx.x * AO_TA + a_l, mu = blockIdx.y * AO_TM + m_l;
+  const bool live = (al < NBA) && (mu < nbas);
   const long long MK = (long long)NBA * nbas;
-  if (t >= nrows_pad) return;
-  const __half hz = __float2half_rn(0.0f);
   const size_t kstride = (size_t)nrows_pad * 64;
-  if (t >= MK) {  // padding rows
-    __half *out = slices + (size_t)t * 64;
-    const uint4 z = make_uint4(0, 0, 0, 0);
-    for (int kc = 0; kc < nks; ++kc)
-      for (int q = 0; q < 64; q += 8)
-        for (int sl = 0; sl < nsl; ++sl)
-          *reinterpret_cast<uint4 *>(out + sl * plane + kc * kstride + q) = z;
-    inv_scale[t] = 1.0f;
-    return;
-  }
-  const int al = (int)(t % NBA), mu = (int)(t / NBA);
-  const long long row = (long long)mu + (long long)nbas * al;
-  const double *src = ao + al + (size_t)NBA * mu;  // element nu at src[MK*nu]
-  unsigned long long mxb = 0;
-  float ss = 0.0f;
-  for (int nu = 0; nu < nbas; ++nu) {
-    const unsigned long long bb = (unsigned long long)__double_as_longlong(src[(size_t)MK * nu]);
-    const unsigned long long mag = bb & 0x7FFFFFFFFFFFFFFFull;
-    mxb = mag > mxb ? mag : mxb;
-    const float f = bits_to_float_trunc(mag, 0);
-    ss = fmaf(f, f, ss);
-  }
-  const double mx = __longlong_as_double((long long)mxb);
+  if (blockIdx.x == 0 && blockIdx.y == 0)
+    for (long long t = MK + threadIdx.x; t < nrows_pad; t += blockDim.x) inv_scale[t] = 1.0f;
+  const double *src = ao + (live ? al + (size_t)NBA * mu : 0);  // element nu at src[MK*nu]
   int e = 0;
-  if (mx > 0.0) {
-    const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
-    const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)nbas)) / nrm);
-    e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
-    e = max(-100, min(100, e));
+  if (live) {
+    unsigned long long mxb = 0;
+    float ss = 0.0f;
+    // sixteen independent loads in flight per thread (one 256-byte segment
+    // per warp each): the loop is bound by memory latency, not arithmetic
+    for (int nu0 = 0; nu0 < nbas; nu0 += 16) {
+      double v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = (nu0 + q < nbas) ? src[(size_t)MK * (nu0 + q)] : 0.0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const unsigned long long mag =
+            (unsigned long long)__double_as_longlong(v[q]) & 0x7FFFFFFFFFFFFFFFull;
+        mxb = mag > mxb ? mag : mxb;
+        const float f = bits_to_float_trunc(mag, 0);
+        ss = fmaf(f, f, ss);
+      }
+    }
+    const double mx = __longlong_as_double((long long)mxb);
+    if (mx > 0.0) {
+      const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
+      const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)nbas)) / nrm);
+      e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
+      e = max(-100, min(100, e));
+    }
   }
-  __half *out = slices + (size_t)row * 64;
+  const int rl = m_l + AO_TM * a_l;  // row within the CTA: the 8 mu of one alpha adjacent
+  const int sw = a_l & 7;
+  const __half hz = __float2half_rn(0.0f);
   for (int attempt = 0; attempt < 64; ++attempt) {
     long long n2 = 0;
     for (int kc = 0; kc < nks; ++kc) {
-      // eight values at a time, written as one 16-byte store per slice
-      for (int q0 = 0; q0 < 64; q0 += 8) {
-        __align__(16) __half h0[8], h1[8], h2[8];
+      for (int q00 = 0; q00 < 64; q00 += 16) {
+        double v[16];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int nu = kc * 64 + q0 + q;
-          h0[q] = h1[q] = h2[q] = hz;
-          if (nu < nbas) {
-            float xh, xl;
-            split_double(src[(size_t)MK * nu], e, xh, xl);
-            const float qv = rintf(xh);
-            const float r = (xh - qv) + xl;
-            h0[q] = __float2half_rn(qv);
-            h1[q] = __float2half_rn(r);
-            h2[q] = __float2half_rn(r - __half2float(h1[q]));
-            const int qi = (int)qv;
-            n2 += (long long)qi * qi;
-          }
+        for (int q = 0; q < 16; ++q) {
+          const int nu = kc * 64 + q00 + q;
+          v[q] = (live && nu < nbas) ? src[(size_t)MK * nu] : 0.0;
         }
-        const size_t o = (size_t)kc * kstride + q0;
-        *reinterpret_cast<uint4 *>(out + o) = *reinterpret_cast<const uint4 *>(h0);
-        if (nsl > 1) *reinterpret_cast<uint4 *>(out + plane + o) = *reinterpret_cast<const uint4 *>(h1);
-        if (nsl > 2)
-          *reinterpret_cast<uint4 *>(out + 2 * plane + o) = *reinterpret_cast<const uint4 *>(h2);
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          __align__(16) __half h0[8], h1[8], h2[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int nu = kc * 64 + q00 + 8 * hh + q;
+            h0[q] = h1[q] = h2[q] = hz;
+            if (live && nu < nbas) {
+              float xh, xl;
+              split_double(v[8 * hh + q], e, xh, xl);
+              const float qv = rintf(xh);
+              const float r = (xh - qv) + xl;
+              h0[q] = __float2half_rn(qv);
+              h1[q] = __float2half_rn(r);
+              h2[q] = __float2half_rn(r - __half2float(h1[q]));
+              const int qi = (int)qv;
+              n2 += (long long)qi * qi;
+            }
+          }
+          const int c = ((q00 >> 3) + hh) ^ sw;
+          stage[(0 * AO_ROWS + rl) * 8 + c] = *reinterpret_cast<const uint4 *>(h0);
+          if (nsl > 1) stage[(1 * AO_ROWS + rl) * 8 + c] = *reinterpret_cast<const uint4 *>(h1);
+          if (nsl > 2) stage[(2 * AO_ROWS + rl) * 8 + c] = *reinterpret_cast<const uint4 *>(h2);
+        }
       }
+      __syncthreads();
+      for (int j = threadIdx.x; j < AO_ROWS * 8; j += AO_ROWS) {
+        const int r = j >> 3, c = j & 7;
+        const int ra = r / AO_TM, rm = r % AO_TM;
+        const int gal = blockIdx.x * AO_TA + ra, gmu = blockIdx.y * AO_TM + rm;
+        if (gal < NBA && gmu < nbas) {
+          const size_t row = (size_t)gmu + (size_t)nbas * gal;
+          __half *dst = slices + (size_t)kc * kstride + row * 64 + c * 8;
+          const int sc = c ^ (ra & 7);
+          for (int sl = 0; sl < nsl; ++sl)
+            *reinterpret_cast<uint4 *>(dst + sl * plane) = stage[(sl * AO_ROWS + r) * 8 + sc];
+        }
+      }
+      __syncthreads();
     }
-    if (n2 <= 16777216LL) break;
-    --e;
+    // the norm bound makes a retry rare; the whole CTA repeats the pass with
+    // a smaller scale on the rows that exceeded it
+    const bool over = n2 > 16777216LL;
+    if (!__syncthreads_or(over)) break;
+    if (over) --e;
   }
-  inv_scale[row] = ldexpf(1.0f, -e);
+  if (live) inv_scale[(size_t)mu + (size_t)nbas * al] = ldexpf(1.0f, -e);
 }
 
 }  // namespace
@@ -1543,8 +1579,16 @@ int sliced_ao(SlicedOp &op, const double *ao, int NBA, int nbas, int nsl, cudaSt
   }
   RIMP2_TRY(op.slices.alloc(sizeof(__half) * (size_t)nsl * op.R * 64, s));
   RIMP2_TRY(op.inv.alloc(sizeof(float) * (size_t)op.ncol, s));
-  ao_slice_kernel<<<(unsigned)((op.ncol + 127) / 128), 128, 0, s>>>(
-      ao, NBA, nbas, op.ncol, op.nks, nsl, op.R * 64, op.slices.as<__half>(), op.inv.as<float>());
+  // padding rows [rows, ncol) of every K chunk of every slice plane: the
+  // chunks are equally spaced (ncol rows of 128 bytes) across the planes
+  if (op.ncol > rows)
+    RIMP2_CK(cudaMemset2DAsync(op.slices.as<__half>() + (size_t)rows * 64, (size_t)op.ncol * 128,
+                               0, (size_t)(op.ncol - rows) * 128, (size_t)op.nks * nsl, s));
+  const int smem = nsl * AO_ROWS * 128;
+  RIMP2_CK(cudaFuncSetAttribute(ao_slice_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  dim3 grid((unsigned)((NBA + AO_TA - 1) / AO_TA), (unsigned)((nbas + AO_TM - 1) / AO_TM));
+  ao_slice_kernel<<<grid, AO_ROWS, smem, s>>>(ao, NBA, nbas, op.ncol, op.nks, nsl, op.R * 64,
+                                              op.slices.as<__half>(), op.inv.as<float>());
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;

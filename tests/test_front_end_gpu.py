@@ -51,10 +51,13 @@ def test_device_ao_generators_match_oracle():
     close(dV.cpu().numpy(), O.gen_metric(5, NBA).ravel(order="F"), 1e-13)
 
 
-def test_cholesky_and_solve_blocks():
+@pytest.mark.parametrize("n,m", [(200, 37), (64, 5), (1, 3), (1100, 130)])
+def test_cholesky_and_solve_blocks(n, m):
+    """Several 64-blocks plus a ragged one, exactly one block, a 1x1 metric,
+    and a metric of 18 blocks (the panel GEMM and the lower-triangle trailing
+    update at many sizes)."""
     import torch
     from rimp2_gpu_gb300 import api
-    n, m = 200, 37  # several 64-blocks plus a ragged one
     V = O.gen_metric(8, n)
     dV = t(V)
     api.cholesky_dev(n, dV.data_ptr())
