@@ -137,6 +137,39 @@ int rimp2_steps5to8(const int *nvirt, const int *nocc, const int *noccEOS, const
                     const double *UoccT, const double *UvirtEOST, double *toccEOS,
                     double *tvirtEOS, double *goccEOS, double *gvirtEOS);
 
+/* First-order property integrals (RIMP2.F90:172-251, the driver's
+ * first_order = .TRUE. block, RIMP2.F90:65):
+ *   djik(nvirt,noccEOS,noccEOS,nocctot) from Calpha, UoccEOST, UvirtT and
+ *     CalphaOcc(NBA,nocc,nocctot) transformed by UoccallT(nocctot,nocctot);
+ *   blad(nvirtEOS,nocc,nvirtEOS,nvirt) from Calpha, UoccT, UvirtEOST and
+ *     CalphaVV(NBA,nvirt,nvirt) transformed by UvirtT.
+ * The driver passes UoccT(nocc,nocc) as UoccallT (RIMP2.F90:197), which is
+ * the same matrix when nocctot = nocc.  As in the driver, the CalphaVV DGEMM
+ * sums over the first nocc rows of UvirtT read with leading dimension nocc
+ * (RIMP2.F90:232-235: K = ldb = nocc), so the results equal the reference's.
+ * All intermediates stay on the device. */
+int rimp2_first_order(const int *nvirt, const int *nocc, const int *noccEOS, const int *nvirtEOS,
+                      const int *nocctot, const int *NBA, const double *Calpha,
+                      const double *CalphaOcc, const double *CalphaVV, const double *UoccEOST,
+                      const double *UvirtT, const double *UoccT, const double *UoccallT,
+                      const double *UvirtEOST, double *djik, double *blad);
+
+/* ---- Calpha{1,2}.data files (host only) -----------------------------------
+ * The reference's fragment files: Fortran unformatted sequential records
+ * with 4-byte length markers, read by RIMP2.F90:36-63,190,229,257-360 and
+ * written by generate.F90:75-128,262,308,333-339.  Array records in order
+ * (arrays[k] is record k+1): Calpha, EVocc, EVvirt, UoccEOST, UvirtT, UoccT,
+ * UvirtEOST, CalphaOcc, CalphaVV, toccEOS, tvirtEOS, gvirtEOS, goccEOS,
+ * djik, blad; CalphaOcc, CalphaVV, djik and blad exist only in first-order
+ * files.  hdr = {nvirt, nocc, noccEOS, nvirtEOS, NBA, nocctot}.  Reading: a
+ * NULL array skips its record; the known answers (toccEOS on) may be absent
+ * if their pointers are NULL.  Writing: the file ends at the first NULL
+ * known-answer array.  Records above 2^31-1 bytes: RIMP2_ERR_UNSUPPORTED. */
+int rimp2_datafile_header(const char *path, int *hdr);
+int rimp2_datafile_read(const char *path, int first_order, double *const *arrays);
+int rimp2_datafile_write(const char *path, const int *hdr, int first_order,
+                         const double *const *arrays);
+
 /* ---- energies (no counterpart in the reference: the reference stops at the
  * amplitudes toccEOS/tvirtEOS and integrals goccEOS/gvirtEOS; the energy is
  * the closed-shell MP2 expression built from the same g and denominator as

@@ -60,6 +60,8 @@ def lib():
                 "orc_gen4dimfo": [i, _dp, i, i, _dp, i, i, _dp],
                 "orc_dgemm": [C.c_char, C.c_char, i, i, i, d, _dp, i, _dp, i, d, _dp, i],
                 "orc_steps5to8": [i, i, i, i, i] + [_dp] * 11,
+                "orc_first_order": [i] * 6 + [_dp] * 10,
+                "orc_gen_kat_fo": [i] * 4 + [_dp] * 2,
                 "orc_pair_energies": [i, i, i, _dp, _dp, _dp, _dp, _ip, i],
                 "orc_pair_energies_blocked": [i, i, i, _dp, _dp, _dp, _dp, _ip, i],
                 "orc_amplitudes": [i, i, i, _dp, _dp, _dp, _dp],
@@ -85,7 +87,7 @@ def lib():
                 "orc_set_num_threads": [i],
             }
             ret = {"orc_pair_energies": d, "orc_pair_energies_blocked": d, "orc_uniform": d,
-                   "orc_normal": d, "orc_steps5to8": i, "orc_write_datafile": i,
+                   "orc_normal": d, "orc_steps5to8": i, "orc_first_order": i, "orc_write_datafile": i,
                    "orc_read_header": i, "orc_read_datafile": i, "orc_cholesky": i,
                    "orc_num_threads": i}
             for name, args in sig.items():
@@ -177,6 +179,21 @@ def steps5to8(nvirt, nocc, noccEOS, nvirtEOS, NBA, Calpha, EVocc, EVvirt, UoccEO
 
 # --- energies ----------------------------------------------------------------
 
+def first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, Calpha, CalphaOcc, CalphaVV,
+                UoccEOST, UvirtT, UoccT, UvirtEOST, UoccallT=None):
+    """First-order block of the driver (RIMP2.F90:172-251): (djik, blad)."""
+    if UoccallT is None:
+        UoccallT = UoccT
+    djik = fzeros(nvirt, noccEOS, noccEOS, nocctot)
+    blad = fzeros(nvirtEOS, nocc, nvirtEOS, nvirt)
+    rc = lib().orc_first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, _p(Calpha),
+                               _p(CalphaOcc), _p(CalphaVV), _p(UoccEOST), _p(UvirtT), _p(UoccT),
+                               _p(UoccallT), _p(UvirtEOST), _p(djik), _p(blad))
+    if rc:
+        raise MemoryError("oracle first_order allocation failed")
+    return djik, blad
+
+
 def _pairs_arg(pairs):
     if pairs is None:
         return None, 0, None
@@ -259,6 +276,14 @@ def gen_kat(NBA, nvirt, nocc, noccEOS, nvirtEOS):
     lib().orc_gen_kat(NBA, nvirt, nocc, noccEOS, nvirtEOS, _p(Ca), _p(eo), _p(ev), _p(UoE), _p(UvT),
                       _p(UoT), _p(UvE))
     return Ca, eo, ev, UoE, UvT, UoT, UvE
+
+
+def gen_kat_fo(NBA, nvirt, nocc, nocctot):
+    """First-order fixture inputs of generate.F90:254-260,300-306."""
+    occ = fzeros(NBA, nocc, nocctot)
+    vv = fzeros(NBA, nvirt, nvirt)
+    lib().orc_gen_kat_fo(NBA, nvirt, nocc, nocctot, _p(occ), _p(vv))
+    return occ, vv
 
 
 def write_datafile(path, nvirt, nocc, noccEOS, nvirtEOS, NBA, nocctot, Calpha, EVocc, EVvirt,

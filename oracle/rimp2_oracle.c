@@ -282,6 +282,48 @@ int orc_steps5to8(int nvirt, int nocc, int noccEOS, int nvirtEOS, int NBA, const
   return 0;
 }
 
+/* First-order property integrals of the driver (RIMP2.F90:172-251, run when
+ * first_order = .TRUE., RIMP2.F90:65; same sequence in generate.F90:237-331).
+ * djik(nvirt,noccEOS,noccEOS,nocctot), blad(nvirtEOS,nocc,nvirtEOS,nvirt).
+ * UoccallT is the (nocctot,nocctot) matrix the djik DGEMM reads
+ * (RIMP2.F90:192-197 passes UoccT there, which is the same array when
+ * nocctot = nocc).  The CalphaVV DGEMM keeps the driver's K = ldb = nocc
+ * (RIMP2.F90:232-235). */
+int orc_first_order(int nvirt, int nocc, int noccEOS, int nvirtEOS, int nocctot, int NBA,
+                    const double *Calpha, const double *CalphaOcc, const double *CalphaVV,
+                    const double *UoccEOST, const double *UvirtT, const double *UoccT,
+                    const double *UoccallT, const double *UvirtEOST, double *djik, double *blad) {
+  size_t nv = nvirt, no = nocc, noE = noccEOS, nvE = nvirtEOS, nb = NBA, nt = nocctot;
+  size_t big = nb * nv * (nv > no ? nv : no);
+  if (nb * no * nt > big) big = nb * no * nt;
+  double *C2 = (double *)malloc(sizeof(double) * big);
+  double *C3 = (double *)malloc(sizeof(double) * big);
+  double *C4 = (double *)malloc(sizeof(double) * big);
+  if (!C2 || !C3 || !C4) return 1;
+  /* djik: RIMP2.F90:177-207 */
+  orc_dgemm('N', 'N', NBA * nvirt, noccEOS, nocc, 1.0, Calpha, NBA * nvirt, UoccEOST, nocc, 0.0, C2,
+            NBA * nvirt);                                            /* :177-182 */
+  orc_transalpha2(noccEOS, nvirt, nvirt, NBA, UvirtT, C2, C3);      /* :186 */
+  orc_dgemm('N', 'N', NBA * nocc, nocctot, nocctot, 1.0, CalphaOcc, NBA * nocc, UoccallT, nocctot,
+            0.0, C2, NBA * nocc);                                    /* :192-197 */
+  orc_transalpha2(nocctot, nocc, noccEOS, NBA, UoccEOST, C2, C4);   /* :201 */
+  orc_gen4dimfo(NBA, C3, nvirt, noccEOS, C4, noccEOS, nocctot, djik); /* :207 */
+  /* blad: RIMP2.F90:216-248 */
+  orc_dgemm('N', 'N', NBA * nvirt, nocc, nocc, 1.0, Calpha, NBA * nvirt, UoccT, nocc, 0.0, C2,
+            NBA * nvirt);                                            /* :216-220 */
+  orc_transalpha2(nocc, nvirt, nvirtEOS, NBA, UvirtEOST, C2, C3);   /* :225 */
+  orc_dgemm('N', 'N', NBA * nvirt, nvirt, nocc, 1.0, CalphaVV, NBA * nvirt, UvirtT, nocc, 0.0, C2,
+            NBA * nvirt);                                            /* :232-235 */
+  orc_transalpha2(nvirt, nvirt, nvirtEOS, NBA, UvirtEOST, C2, C4);  /* :242 */
+  orc_gen4dimfo(NBA, C3, nvirtEOS, nocc, C4, nvirtEOS, nvirt, blad); /* :248 */
+  free(C2);
+  free(C3);
+  free(C4);
+  (void)noE;
+  (void)nvE;
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* MP2 pair energies (restated; no counterpart in the reference)            */
 /* ------------------------------------------------------------------------ */
@@ -588,6 +630,20 @@ void orc_gen_kat(int NBA, int nvirt, int nocc, int noccEOS, int nvirtEOS, double
   for (int b = 1; b <= nvirtEOS; ++b)
     for (int a = 1; a <= nvirt; ++a)
       UvirtEOST[I2(a - 1, b - 1, nvirt)] = a * 0.023321 / a + b * 0.01421 / b; /* :125 */
+}
+
+/* First-order fixture inputs of generate.F90:254-260 (CalphaOcc) and
+ * :300-306 (CalphaVV): A*0.01124235636 + B*0.01011111 + C*0.16422. */
+void orc_gen_kat_fo(int NBA, int nvirt, int nocc, int nocctot, double *CalphaOcc,
+                    double *CalphaVV) {
+  for (int c = 1; c <= nocctot; ++c)
+    for (int b = 1; b <= nocc; ++b)
+      for (int a = 1; a <= NBA; ++a)
+        CalphaOcc[I3(a - 1, b - 1, c - 1, NBA, nocc)] = a * 0.01124235636 + b * 0.01011111 + c * 0.16422;
+  for (int c = 1; c <= nvirt; ++c)
+    for (int b = 1; b <= nvirt; ++b)
+      for (int a = 1; a <= NBA; ++a)
+        CalphaVV[I3(a - 1, b - 1, c - 1, NBA, nvirt)] = a * 0.01124235636 + b * 0.01011111 + c * 0.16422;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -126,6 +126,85 @@ def steps5to8(nvirt, nocc, noccEOS, nvirtEOS, NBA, Calpha, EVocc, EVvirt, UoccEO
     return toccEOS, tvirtEOS, goccEOS, gvirtEOS
 
 
+def first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, Calpha, CalphaOcc, CalphaVV,
+                UoccEOST, UvirtT, UoccT, UvirtEOST, UoccallT=None):
+    """First-order property integrals of the driver (RIMP2.F90:172-251) on
+    the GPU; returns (djik, blad).  UoccallT defaults to UoccT, as the driver
+    passes it (RIMP2.F90:197)."""
+    if UoccallT is None:
+        UoccallT = UoccT
+    f = lambda *s: np.zeros(s, dtype=np.float64, order="F")  # noqa: E731
+    djik = f(nvirt, noccEOS, noccEOS, nocctot)
+    blad = f(nvirtEOS, nocc, nvirtEOS, nvirt)
+    call("rimp2_first_order", _i(nvirt), _i(nocc), _i(noccEOS), _i(nvirtEOS), _i(nocctot), _i(NBA),
+         _a(Calpha, "Calpha", (NBA, nvirt, nocc)),
+         _a(CalphaOcc, "CalphaOcc", (NBA, nocc, nocctot)),
+         _a(CalphaVV, "CalphaVV", (NBA, nvirt, nvirt)), _a(UoccEOST, "UoccEOST", (nocc, noccEOS)),
+         _a(UvirtT, "UvirtT", (nvirt, nvirt)), _a(UoccT, "UoccT", (nocc, nocc)),
+         _a(UoccallT, "UoccallT", (nocctot, nocctot)), _a(UvirtEOST, "UvirtEOST", (nvirt, nvirtEOS)),
+         _a(djik, "djik", writable=True), _a(blad, "blad", writable=True))
+    return djik, blad
+
+
+DATAFILE_RECORDS = ("Calpha", "EVocc", "EVvirt", "UoccEOST", "UvirtT", "UoccT", "UvirtEOST",
+                    "CalphaOcc", "CalphaVV", "toccEOS", "tvirtEOS", "gvirtEOS", "goccEOS",
+                    "djik", "blad")
+_FIRST_ORDER_ONLY = {"CalphaOcc", "CalphaVV", "djik", "blad"}
+
+
+def _datafile_shapes(nvirt, nocc, noccEOS, nvirtEOS, NBA, nocctot):
+    return dict(Calpha=(NBA, nvirt, nocc), EVocc=(nocc,), EVvirt=(nvirt,),
+                UoccEOST=(nocc, noccEOS), UvirtT=(nvirt, nvirt), UoccT=(nocc, nocc),
+                UvirtEOST=(nvirt, nvirtEOS), CalphaOcc=(NBA, nocc, nocctot),
+                CalphaVV=(NBA, nvirt, nvirt), toccEOS=(nvirt, noccEOS, nvirt, noccEOS),
+                tvirtEOS=(nvirtEOS, nocc, nvirtEOS, nocc),
+                gvirtEOS=(nvirtEOS, nocc, nvirtEOS, nocc),
+                goccEOS=(nvirt, noccEOS, nvirt, noccEOS), djik=(nvirt, noccEOS, noccEOS, nocctot),
+                blad=(nvirtEOS, nocc, nvirtEOS, nvirt))
+
+
+def read_datafile(path, first_order=False, known_answers=True):
+    """Read a Calpha{1,2}.data file (C-ABI rimp2_datafile_read); returns a
+    dict of the header dimensions and Fortran-ordered arrays.  With
+    known_answers=False the test records (toccEOS on) are skipped."""
+    h = (C.c_int * 6)()
+    call("rimp2_datafile_header", str(path).encode(), h)
+    dims = dict(zip(("nvirt", "nocc", "noccEOS", "nvirtEOS", "NBA", "nocctot"), list(h)))
+    shapes = _datafile_shapes(**dims)
+    out = dict(dims)
+    ptrs = (C.c_void_p * len(DATAFILE_RECORDS))()
+    for k, name in enumerate(DATAFILE_RECORDS):
+        if name in _FIRST_ORDER_ONLY and not first_order:
+            continue
+        if k >= 9 and not known_answers:
+            continue
+        a = np.zeros(shapes[name], dtype=np.float64, order="F")
+        out[name] = a
+        ptrs[k] = a.ctypes.data
+    call("rimp2_datafile_read", str(path).encode(), 1 if first_order else 0, ptrs)
+    return out
+
+
+def write_datafile(path, arrays, first_order=False):
+    """Write a Calpha{1,2}.data file from a dict holding the header
+    dimensions and the arrays (C-ABI rimp2_datafile_write)."""
+    dims = [int(arrays[k]) for k in ("nvirt", "nocc", "noccEOS", "nvirtEOS", "NBA", "nocctot")]
+    shapes = _datafile_shapes(*dims)
+    ptrs = (C.c_void_p * len(DATAFILE_RECORDS))()
+    keep = []
+    for k, name in enumerate(DATAFILE_RECORDS):
+        a = arrays.get(name)
+        if a is None:
+            continue
+        a = np.asfortranarray(a, dtype=np.float64)
+        if a.size != int(np.prod(shapes[name])):
+            raise ValueError(f"{name} has {a.size} elements, expected {shapes[name]}")
+        keep.append(a)
+        ptrs[k] = a.ctypes.data
+    call("rimp2_datafile_write", str(path).encode(), (C.c_int * 6)(*dims),
+         1 if first_order else 0, ptrs)
+
+
 def energy(nvirt, nocc, NBA, Calpha, EVocc, EVvirt, precision=PREC_FP64, amplitudes=False):
     """MP2 pair energies and total from host arrays (C-ABI rimp2_energy).
     Returns (Epair[nocc,nocc], Etot[, tamp(nvirt,nocc,nvirt,nocc)])."""

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librimp2_gpu_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "fp64_kernels.cu", "split_kernels.cu", "front_end.cu", "synth.cu", "noalloc.cu"]
+SOURCES = ["capi.cu", "fp64_kernels.cu", "split_kernels.cu", "front_end.cu", "synth.cu", "noalloc.cu",
+           "datafile.cu"]
 
 
 def nvcc() -> str:

@@ -681,6 +681,79 @@ int rimp2_steps5to8(const int *nvirt_, const int *nocc_, const int *noccEOS_, co
   return finish(s);
 }
 
+int rimp2_first_order(const int *nvirt_, const int *nocc_, const int *noccEOS_,
+                      const int *nvirtEOS_, const int *nocctot_, const int *NBA_,
+                      const double *Calpha, const double *CalphaOcc, const double *CalphaVV,
+                      const double *UoccEOST, const double *UvirtT, const double *UoccT,
+                      const double *UoccallT, const double *UvirtEOST, double *djik,
+                      double *blad) {
+  clear_error();
+  RIMP2_REQ(pos(nvirt_) && pos(nocc_) && pos(noccEOS_) && pos(nvirtEOS_) && pos(nocctot_) &&
+                pos(NBA_),
+            "rimp2_first_order: bad dims");
+  RIMP2_REQ(Calpha && CalphaOcc && CalphaVV && UoccEOST && UvirtT && UoccT && UoccallT &&
+                UvirtEOST && djik && blad,
+            "rimp2_first_order: null array");
+  RIMP2_REQ(*nocc_ <= *nvirt_,
+            "rimp2_first_order: nocc > nvirt (the CalphaVV DGEMM reads nocc rows of UvirtT)");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const int nvirt = *nvirt_, nocc = *nocc_, noccEOS = *noccEOS_, nvirtEOS = *nvirtEOS_,
+            nocctot = *nocctot_, NBA = *NBA_;
+  const size_t nv = nvirt, no = nocc, ne = noccEOS, ve = nvirtEOS, nt = nocctot, nb = NBA;
+  DevBuf dC, dUoE, dUvT, dUoT, dUoA, dUvE;
+  RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
+  RIMP2_TRY(h2d(dUoE, UoccEOST, no * ne, s));
+  RIMP2_TRY(h2d(dUvT, UvirtT, nv * nv, s));
+  RIMP2_TRY(h2d(dUoT, UoccT, no * no, s));
+  RIMP2_TRY(h2d(dUoA, UoccallT, nt * nt, s));
+  RIMP2_TRY(h2d(dUvE, UvirtEOST, nv * ve, s));
+  const double *Ca = dC.as<double>();
+  {  // djik (RIMP2.F90:177-207)
+    DevBuf dOcc, c2, c3, c2b, c4, out;
+    RIMP2_TRY(h2d(dOcc, CalphaOcc, nb * no * nt, s));
+    RIMP2_TRY(dalloc(c2, nb * nv * ne, s));
+    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nvirt, noccEOS, nocc, 1.0, Ca, NBA * nvirt,
+                        dUoE.as<double>(), nocc, 0.0, c2.as<double>(), NBA * nvirt, s));
+    RIMP2_TRY(dalloc(c3, nb * nv * ne, s));
+    RIMP2_TRY(dev_transalpha2(noccEOS, nvirt, nvirt, NBA, dUvT.as<double>(), c2.as<double>(),
+                              c3.as<double>(), s));
+    RIMP2_TRY(dalloc(c2b, nb * no * nt, s));
+    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nocc, nocctot, nocctot, 1.0, dOcc.as<double>(), NBA * nocc,
+                        dUoA.as<double>(), nocctot, 0.0, c2b.as<double>(), NBA * nocc, s));
+    RIMP2_TRY(dalloc(c4, nb * ne * nt, s));
+    RIMP2_TRY(dev_transalpha2(nocctot, nocc, noccEOS, NBA, dUoE.as<double>(), c2b.as<double>(),
+                              c4.as<double>(), s));
+    RIMP2_TRY(dalloc(out, nv * ne * ne * nt, s));
+    RIMP2_TRY(dev_gen4dimfo(NBA, c3.as<double>(), nvirt, noccEOS, c4.as<double>(), noccEOS, nocctot,
+                            out.as<double>(), s));
+    RIMP2_TRY(d2h(djik, out, nv * ne * ne * nt, s));
+    RIMP2_CK(cudaStreamSynchronize(s));
+  }
+  {  // blad (RIMP2.F90:216-248)
+    DevBuf dVV, c2, c3, c2b, c4, out;
+    RIMP2_TRY(dalloc(c2, nb * nv * no, s));
+    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nvirt, nocc, nocc, 1.0, Ca, NBA * nvirt, dUoT.as<double>(),
+                        nocc, 0.0, c2.as<double>(), NBA * nvirt, s));
+    RIMP2_TRY(dalloc(c3, nb * ve * no, s));
+    RIMP2_TRY(dev_transalpha2(nocc, nvirt, nvirtEOS, NBA, dUvE.as<double>(), c2.as<double>(),
+                              c3.as<double>(), s));
+    RIMP2_TRY(h2d(dVV, CalphaVV, nb * nv * nv, s));
+    RIMP2_TRY(dalloc(c2b, nb * nv * nv, s));
+    // K = ldb = nocc as in the driver's DGEMM (RIMP2.F90:232-235)
+    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nvirt, nvirt, nocc, 1.0, dVV.as<double>(), NBA * nvirt,
+                        dUvT.as<double>(), nocc, 0.0, c2b.as<double>(), NBA * nvirt, s));
+    RIMP2_TRY(dalloc(c4, nb * ve * nv, s));
+    RIMP2_TRY(dev_transalpha2(nvirt, nvirt, nvirtEOS, NBA, dUvE.as<double>(), c2b.as<double>(),
+                              c4.as<double>(), s));
+    RIMP2_TRY(dalloc(out, ve * no * ve * nv, s));
+    RIMP2_TRY(dev_gen4dimfo(NBA, c3.as<double>(), nvirtEOS, nocc, c4.as<double>(), nvirtEOS, nvirt,
+                            out.as<double>(), s));
+    RIMP2_TRY(d2h(blad, out, ve * no * ve * nv, s));
+  }
+  return finish(s);
+}
+
 int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const double *dEVocc,
                      const double *dEVvirt, double *dEpair, double *dEtot, double *dtamp,
                      int precision, void *stream) {

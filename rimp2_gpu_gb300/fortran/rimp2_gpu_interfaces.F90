@@ -128,6 +128,20 @@ module rimp2_gpu_interfaces
        real(C_DOUBLE), intent(inout) :: gvirtEOS(nvirtEOS,nocc,nvirtEOS,nocc)
      end function rimp2_steps5to8
 
+     ! first-order block of the driver (RIMP2.F90:172-251); pass UoccT as UoccallT
+     integer(C_INT) function rimp2_first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, &
+          & Calpha, CalphaOcc, CalphaVV, UoccEOST, UvirtT, UoccT, UoccallT, UvirtEOST, djik, blad) &
+          & bind(C, name="rimp2_first_order")
+       import :: C_INT, C_DOUBLE
+       integer(C_INT), intent(in) :: nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA
+       real(C_DOUBLE), intent(in) :: Calpha(NBA,nvirt,nocc), CalphaOcc(NBA,nocc,nocctot)
+       real(C_DOUBLE), intent(in) :: CalphaVV(NBA,nvirt,nvirt), UoccEOST(nocc,noccEOS)
+       real(C_DOUBLE), intent(in) :: UvirtT(nvirt,nvirt), UoccT(nocc,nocc)
+       real(C_DOUBLE), intent(in) :: UoccallT(nocctot,nocctot), UvirtEOST(nvirt,nvirtEOS)
+       real(C_DOUBLE), intent(inout) :: djik(nvirt,noccEOS,noccEOS,nocctot)
+       real(C_DOUBLE), intent(inout) :: blad(nvirtEOS,nocc,nvirtEOS,nvirt)
+     end function rimp2_first_order
+
      ! MP2 pair and total energy (FP64 or split precision); tamp may be C_NULL_PTR
      integer(C_INT) function rimp2_energy(nvirt, nocc, NBA, Calpha, EVocc, EVvirt, Epair, Etot, &
           & tamp, precision) bind(C, name="rimp2_energy")

@@ -17,6 +17,12 @@ inputs (the generators use libm, whose last bits may differ across hosts).
                       stored checksums.
   kat.npz           : outputs of the constant-valued fixtures of
                       generate.F90:77-128 at both shipped sizes.
+  first_order.npz   : the driver's first-order block (RIMP2.F90:172-251):
+                      djik and blad of a small case with random non-unitary
+                      matrices and nocctot != nocc (a separate UoccallT), and
+                      the min/max of djik and blad from the generate.F90
+                      first-order fixture inputs (:254-260,300-306) at both
+                      shipped sizes (every element is the same constant).
 """
 import os
 import sys
@@ -75,8 +81,37 @@ def kat():
     np.savez_compressed(os.path.join(HERE, "kat.npz"), **out)
 
 
+def first_order():
+    nvirt, nocc, noccEOS, nvirtEOS, NBA, nocctot = 21, 5, 3, 7, 37, 8
+    seed = 12
+    Ca = O.gen_calpha(seed, NBA, nvirt, nocc)
+    occ = O.gen_matrix(seed, 20, NBA * nocc, nocctot).reshape(NBA, nocc, nocctot, order="F")
+    vv = O.gen_matrix(seed, 21, NBA * nvirt, nvirt).reshape(NBA, nvirt, nvirt, order="F")
+    UoE = O.gen_matrix(seed, 10, nocc, noccEOS)
+    UvT = O.gen_matrix(seed, 11, nvirt, nvirt)
+    UoT = O.gen_matrix(seed, 12, nocc, nocc)
+    UoA = O.gen_matrix(seed, 14, nocctot, nocctot)
+    UvE = O.gen_matrix(seed, 13, nvirt, nvirtEOS)
+    occ, vv = np.asfortranarray(occ), np.asfortranarray(vv)
+    djik, blad = O.first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, Ca, occ, vv, UoE, UvT,
+                               UoT, UvE, UoccallT=UoA)
+    out = dict(nvirt=nvirt, nocc=nocc, noccEOS=noccEOS, nvirtEOS=nvirtEOS, NBA=NBA, nocctot=nocctot,
+               Calpha=Ca, CalphaOcc=occ, CalphaVV=vv, UoccEOST=UoE, UvirtT=UvT, UoccT=UoT,
+               UoccallT=UoA, UvirtEOST=UvE, djik=djik, blad=blad)
+    for k, (nvirt, nocc, noccEOS, nvirtEOS, NBA) in enumerate([(74, 10, 4, 15, 273),
+                                                                (104, 20, 4, 15, 373)], 1):
+        Ca, eo, ev, UoE, UvT, UoT, UvE = O.gen_kat(NBA, nvirt, nocc, noccEOS, nvirtEOS)
+        occ, vv = O.gen_kat_fo(NBA, nvirt, nocc, nocc)
+        d, b = O.first_order(nvirt, nocc, noccEOS, nvirtEOS, nocc, NBA, Ca, occ, vv, UoE, UvT, UoT,
+                             UvE)
+        out[f"file{k}_djik"] = np.array([d.min(), d.max()])
+        out[f"file{k}_blad"] = np.array([b.min(), b.max()])
+    np.savez_compressed(os.path.join(HERE, "first_order.npz"), **out)
+
+
 if __name__ == "__main__":
     small_general()
     energy_cfg1()
+    first_order()
     kat()
     print("golden fixtures written to", HERE)

@@ -83,3 +83,101 @@ def test_default_buckets_match_committed_tuning_table():
             assert api.split_nslices(max(nv, 1), 8, 256) == b["nslices"] or any(
                 c["nvirt_min"] <= nv and c["nvirt_min"] > b["nvirt_min"] for c in t["buckets"])
         assert b["worst_rel_err"][str(b["nslices"])] <= t["target"] * t["margin"]
+
+
+def _raw_records(path):
+    """Split a Fortran unformatted sequential file into its records."""
+    out, b = [], open(path, "rb").read()
+    p = 0
+    while p < len(b):
+        n = int(np.frombuffer(b, np.int32, 1, p)[0])
+        out.append(b[p + 4:p + 4 + n])
+        assert int(np.frombuffer(b, np.int32, 1, p + 4 + n)[0]) == n
+        p += 8 + n
+    return out
+
+
+def test_datafile_reads_oracle_written_file(tmp_path):
+    """The library reads a Calpha{1,2}.data file written in the record order
+    of generate.F90:75-128,333-336 by the oracle."""
+    from oracle import oracle as O
+    from rimp2_gpu_gb300 import api
+    nvirt, nocc, noccEOS, nvirtEOS, NBA = 7, 3, 2, 4, 11
+    arrs = O.gen_kat(NBA, nvirt, nocc, noccEOS, nvirtEOS)
+    outs = O.steps5to8(nvirt, nocc, noccEOS, nvirtEOS, NBA, *arrs)
+    path = str(tmp_path / "Calpha1.data")
+    O.write_datafile(path, nvirt, nocc, noccEOS, nvirtEOS, NBA, nocc, *arrs, outs[0], outs[1],
+                     outs[3], outs[2])
+    d = api.read_datafile(path)
+    assert (d["nvirt"], d["nocc"], d["noccEOS"], d["nvirtEOS"], d["NBA"], d["nocctot"]) == \
+        (nvirt, nocc, noccEOS, nvirtEOS, NBA, nocc)
+    for name, a in zip(("Calpha", "EVocc", "EVvirt", "UoccEOST", "UvirtT", "UoccT", "UvirtEOST"),
+                       arrs):
+        np.testing.assert_array_equal(d[name], a)
+    np.testing.assert_array_equal(d["toccEOS"], outs[0])
+    np.testing.assert_array_equal(d["tvirtEOS"], outs[1])
+    np.testing.assert_array_equal(d["goccEOS"], outs[2])
+    np.testing.assert_array_equal(d["gvirtEOS"], outs[3])
+    # inputs only: the known-answer records are skipped
+    d2 = api.read_datafile(path, known_answers=False)
+    assert "toccEOS" not in d2
+    np.testing.assert_array_equal(d2["Calpha"], arrs[0])
+
+
+def test_datafile_first_order_roundtrip_and_layout(tmp_path):
+    """First-order files: CalphaOcc/CalphaVV after UvirtEOST and djik/blad
+    after goccEOS (generate.F90:262,308,333-339); the library writes them
+    and reads them back, and the raw records are in that order."""
+    from oracle import oracle as O
+    from rimp2_gpu_gb300 import api
+    nvirt, nocc, noccEOS, nvirtEOS, NBA = 9, 4, 2, 3, 13
+    Ca, eo, ev, UoE, UvT, UoT, UvE = O.gen_kat(NBA, nvirt, nocc, noccEOS, nvirtEOS)
+    occ, vv = O.gen_kat_fo(NBA, nvirt, nocc, nocc)
+    tE, vE, gE, gvE = O.steps5to8(nvirt, nocc, noccEOS, nvirtEOS, NBA, Ca, eo, ev, UoE, UvT, UoT,
+                                  UvE)
+    djik, blad = O.first_order(nvirt, nocc, noccEOS, nvirtEOS, nocc, NBA, Ca, occ, vv, UoE, UvT,
+                               UoT, UvE)
+    arrays = dict(nvirt=nvirt, nocc=nocc, noccEOS=noccEOS, nvirtEOS=nvirtEOS, NBA=NBA,
+                  nocctot=nocc, Calpha=Ca, EVocc=eo, EVvirt=ev, UoccEOST=UoE, UvirtT=UvT,
+                  UoccT=UoT, UvirtEOST=UvE, CalphaOcc=occ, CalphaVV=vv, toccEOS=tE,
+                  tvirtEOS=vE, gvirtEOS=gvE, goccEOS=gE, djik=djik, blad=blad)
+    path = str(tmp_path / "Calpha2.data")
+    api.write_datafile(path, arrays, first_order=True)
+    recs = _raw_records(path)
+    assert len(recs) == 16
+    np.testing.assert_array_equal(np.frombuffer(recs[0], np.int32),
+                                  [nvirt, nocc, noccEOS, nvirtEOS, NBA, nocc])
+    order = ["Calpha", "EVocc", "EVvirt", "UoccEOST", "UvirtT", "UoccT", "UvirtEOST", "CalphaOcc",
+             "CalphaVV", "toccEOS", "tvirtEOS", "gvirtEOS", "goccEOS", "djik", "blad"]
+    for rec, name in zip(recs[1:], order):
+        np.testing.assert_array_equal(np.frombuffer(rec, np.float64),
+                                      np.asarray(arrays[name]).ravel(order="F"))
+    d = api.read_datafile(path, first_order=True)
+    for name in order:
+        np.testing.assert_array_equal(d[name], arrays[name])
+
+
+def test_datafile_rejects_bad_files(tmp_path):
+    from rimp2_gpu_gb300 import api, _lib
+    good = tmp_path / "ok.data"
+    Ca = np.zeros((5, 3, 2), order="F")
+    arrays = dict(nvirt=3, nocc=2, noccEOS=1, nvirtEOS=1, NBA=5, nocctot=2, Calpha=Ca,
+                  EVocc=np.zeros(2), EVvirt=np.zeros(3), UoccEOST=np.zeros((2, 1)),
+                  UvirtT=np.zeros((3, 3)), UoccT=np.zeros((2, 2)), UvirtEOST=np.zeros((3, 1)))
+    api.write_datafile(str(good), arrays)
+    d = api.read_datafile(str(good), known_answers=False)
+    assert d["Calpha"].shape == (5, 3, 2)
+    with pytest.raises(_lib.Rimp2Error):  # known answers requested but absent
+        api.read_datafile(str(good))
+    b = bytearray(good.read_bytes())
+    bad = tmp_path / "bad.data"
+    bad.write_bytes(bytes(b[:len(b) - 10]))  # truncated
+    with pytest.raises(_lib.Rimp2Error):
+        api.read_datafile(str(bad), known_answers=False)
+    b[32] ^= 0xFF  # corrupt the Calpha record's length marker
+    bad.write_bytes(bytes(b))
+    with pytest.raises(_lib.Rimp2Error) as ei:
+        api.read_datafile(str(bad), known_answers=False)
+    assert ei.value.status == 1
+    with pytest.raises(_lib.Rimp2Error):
+        api.read_datafile(str(tmp_path / "missing.data"))

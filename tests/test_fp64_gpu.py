@@ -153,6 +153,46 @@ def test_steps5to8_reference_known_answers(api, k):
         assert np.abs(arr - exp[name]).max() <= 1e-10, name
 
 
+@pytest.mark.parametrize("k", [0, 1])
+def test_first_order_reference_known_answers(api, k):
+    """The driver's first-order block (RIMP2.F90:172-251) on generate.F90's
+    first-order inputs, with the reference's 1e-10 check (RIMP2.F90:337,355)
+    against the closed forms."""
+    from tests.test_oracle import SIZES, first_order_closed_forms
+    nvirt, nocc, noccEOS, nvirtEOS, NBA = SIZES[k]
+    Ca, _, _, UoE, UvT, UoT, UvE = O.gen_kat(NBA, nvirt, nocc, noccEOS, nvirtEOS)
+    occ, vv = O.gen_kat_fo(NBA, nvirt, nocc, nocc)
+    djik, blad = api.first_order(nvirt, nocc, noccEOS, nvirtEOS, nocc, NBA, Ca, occ, vv, UoE, UvT,
+                                 UoT, UvE)
+    d_exp, b_exp = first_order_closed_forms(nvirt, nocc, noccEOS, nvirtEOS, NBA, nocc)
+    assert np.abs(djik - d_exp).max() <= 1e-10
+    assert np.abs(blad - b_exp).max() <= 1e-10
+
+
+def test_first_order_golden_general(api, golden):
+    """Random non-unitary matrices, nocctot != nocc with a separate UoccallT."""
+    g = golden("first_order.npz")
+    nv, no, ne, ve, nb, nt = (int(g[k]) for k in ("nvirt", "nocc", "noccEOS", "nvirtEOS", "NBA",
+                                                 "nocctot"))
+    A = {k: np.asfortranarray(g[k]) for k in ("Calpha", "CalphaOcc", "CalphaVV", "UoccEOST",
+                                              "UvirtT", "UoccT", "UoccallT", "UvirtEOST")}
+    djik, blad = api.first_order(nv, no, ne, ve, nt, nb, A["Calpha"], A["CalphaOcc"],
+                                 A["CalphaVV"], A["UoccEOST"], A["UvirtT"], A["UoccT"],
+                                 A["UvirtEOST"], UoccallT=A["UoccallT"])
+    close(djik, g["djik"])
+    close(blad, g["blad"])
+
+
+def test_first_order_rejects_nocc_above_nvirt(api):
+    from rimp2_gpu_gb300 import _lib
+    nv, no, ne, ve, nb = 3, 4, 2, 2, 5
+    z = lambda *s: np.zeros(s, order="F")  # noqa: E731
+    with pytest.raises(_lib.Rimp2Error) as ei:
+        api.first_order(nv, no, ne, ve, no, nb, z(nb, nv, no), z(nb, no, no), z(nb, nv, nv),
+                        z(no, ne), z(nv, nv), z(no, no), z(nv, ve))
+    assert ei.value.status == 1
+
+
 def test_get_dev_mem(api):
     total, free = api.get_dev_mem()
     assert total > 200e9 and 0 < free <= total

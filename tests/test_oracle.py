@@ -45,6 +45,74 @@ def test_reference_known_answers(k, golden):
         np.testing.assert_array_equal(np.array([arr.min(), arr.max()]), g[f"file{k+1}_{name}"])
 
 
+# first-order fixture inputs CalphaOcc/CalphaVV(A,B,C) = A*X + B*Y + C*Z
+# (generate.F90:258,304); djik and blad are constants with closed forms
+FX, FY, FZ = 0.01124235636, 0.01011111, 0.16422
+
+
+def first_order_closed_forms(nvirt, nocc, noccEOS, nvirtEOS, NBA, nocctot):
+    c = C_CONST
+    sa = FX * NBA * (NBA + 1) / 2
+    # djik: Calpha3 = nvirt*UV*c*nocc*U1 (RIMP2.F90:182,186); Calpha4(alpha) =
+    # U1*UO*nocctot*nocc*(alpha X + Y (nocc+1)/2 + Z (nocctot+1)/2) (:197,201)
+    djik = (nvirt * UV * c * nocc * U1) * U1 * UO * nocctot * nocc * (
+        sa + NBA * (FY * (nocc + 1) / 2 + FZ * (nocctot + 1) / 2))
+    # blad: Calpha3 = nvirt*W*c*nocc*UO (:220,225); the CalphaVV DGEMM sums
+    # k = 1..nocc (:232-235): Calpha4(alpha) = W*UV*nocc*nvirt*(alpha X +
+    # Y (nvirt+1)/2 + Z (nocc+1)/2) (:242)
+    blad = (nvirt * W * c * nocc * UO) * W * UV * nocc * nvirt * (
+        sa + NBA * (FY * (nvirt + 1) / 2 + FZ * (nocc + 1) / 2))
+    return djik, blad
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_first_order_known_answers(k, golden):
+    """The driver's first_order block on generate.F90's first-order inputs
+    matches the closed forms within the reference's 1e-10 (RIMP2.F90:337,355)."""
+    nvirt, nocc, noccEOS, nvirtEOS, NBA = SIZES[k]
+    arrs = O.gen_kat(NBA, nvirt, nocc, noccEOS, nvirtEOS)
+    Ca, _, _, UoE, UvT, UoT, UvE = arrs
+    occ, vv = O.gen_kat_fo(NBA, nvirt, nocc, nocc)
+    djik, blad = O.first_order(nvirt, nocc, noccEOS, nvirtEOS, nocc, NBA, Ca, occ, vv, UoE, UvT,
+                               UoT, UvE)
+    d_exp, b_exp = first_order_closed_forms(nvirt, nocc, noccEOS, nvirtEOS, NBA, nocc)
+    assert np.abs(djik - d_exp).max() <= 1e-10
+    assert np.abs(blad - b_exp).max() <= 1e-10
+    g = golden("first_order.npz")
+    np.testing.assert_array_equal(np.array([djik.min(), djik.max()]), g[f"file{k+1}_djik"])
+    np.testing.assert_array_equal(np.array([blad.min(), blad.max()]), g[f"file{k+1}_blad"])
+
+
+def test_first_order_einsum_restatement(golden):
+    """The oracle's first-order sequence against an independent numpy
+    restatement of RIMP2.F90:177-248, with random non-unitary matrices and
+    nocctot != nocc, and against the committed fixture."""
+    g = golden("first_order.npz")
+    nv, no, ne, ve, nb, nt = (int(g[k]) for k in ("nvirt", "nocc", "noccEOS", "nvirtEOS", "NBA",
+                                                 "nocctot"))
+    A = {k: np.asfortranarray(g[k]) for k in ("Calpha", "CalphaOcc", "CalphaVV", "UoccEOST",
+                                              "UvirtT", "UoccT", "UoccallT", "UvirtEOST")}
+    djik, blad = O.first_order(nv, no, ne, ve, nt, nb, A["Calpha"], A["CalphaOcc"], A["CalphaVV"],
+                               A["UoccEOST"], A["UvirtT"], A["UoccT"], A["UvirtEOST"],
+                               UoccallT=A["UoccallT"])
+    Ca = A["Calpha"]
+    c2 = np.einsum("xbj,jl->xbl", Ca, A["UoccEOST"])                     # :182
+    c3 = np.einsum("nm,xnl->xml", A["UvirtT"], c2)                       # :186 TransAlpha2
+    c2b = np.einsum("xbm,mk->xbk", A["CalphaOcc"], A["UoccallT"])        # :197
+    c4 = np.einsum("bl,xbk->xlk", A["UoccEOST"], c2b)                    # :201
+    d_ref = np.einsum("xab,xcd->abcd", c3, c4)                           # :207
+    c2 = np.einsum("xbj,jk->xbk", Ca, A["UoccT"])                        # :220
+    c3 = np.einsum("bm,xbk->xmk", A["UvirtEOST"], c2)                    # :225
+    Uview = A["UvirtT"].ravel(order="F")[:no * nv].reshape(no, nv, order="F")  # K = ldb = nocc
+    c2b = np.einsum("xbk,kn->xbn", A["CalphaVV"][:, :, :no], Uview)     # :232-235
+    c4 = np.einsum("bm,xbn->xmn", A["UvirtEOST"], c2b)                   # :242
+    b_ref = np.einsum("xab,xcd->abcd", c3, c4)                           # :248
+    np.testing.assert_allclose(djik, d_ref, rtol=1e-12, atol=1e-13 * np.abs(d_ref).max())
+    np.testing.assert_allclose(blad, b_ref, rtol=1e-12, atol=1e-13 * np.abs(b_ref).max())
+    np.testing.assert_allclose(djik, g["djik"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(blad, g["blad"], rtol=1e-13, atol=1e-15)
+
+
 def test_golden_small_general_reproduces(golden):
     g = golden("small_general.npz")
     n = {k: int(g[k]) for k in ("nvirt", "nocc", "noccEOS", "nvirtEOS", "NBA")}
