@@ -365,29 +365,33 @@ def run_ours(args):
         api.energy_split_dev(NVIRT, NOCC, NBA, dCa.data_ptr(), deo.data_ptr(), dev_.data_ptr(),
                              dEp.data_ptr(), dEt.data_ptr(), nslices=nsl, stream=sp)
 
+    # ---- warm-up (also brings the clocks up before the FP64 check) ----
+    for _ in range(args.warmup):
+        step()
+    api.sync_status(sp)
+
     # ---- FP64 reference energies on the GPU (plain fused kernel), untimed ----
     plain = None
     if args.check == "full":
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        api.energy_dev(NVIRT, NOCC, NBA, dCa.data_ptr(), deo.data_ptr(), dev_.data_ptr(),
-                       dEp64.data_ptr(), dEt64.data_ptr(), precision=api.PREC_FP64, stream=sp)
-        e1.record(st)
-        st.synchronize()
-        api.sync_status(sp)
-        pms = e0.elapsed_time(e1)
+        # a run shorter than ~2 s is repeated and the second one timed (clock ramp)
+        for rep in range(2):
+            e0.record(st)
+            api.energy_dev(NVIRT, NOCC, NBA, dCa.data_ptr(), deo.data_ptr(), dev_.data_ptr(),
+                           dEp64.data_ptr(), dEt64.data_ptr(), precision=api.PREC_FP64, stream=sp)
+            e1.record(st)
+            st.synchronize()
+            api.sync_status(sp)
+            pms = e0.elapsed_time(e1)
+            if pms > 2000.0:
+                break
         fp64_peak = api.probe_fp64_peak()
         # the plain kernel performs (nocc+1)/(2 nocc) of the effective count
         performed = eff_flop() * (NOCC + 1) / (2 * NOCC)
         plain = {"ms": pms, "eff_tflops": eff_flop() / pms / 1e9,
                  "performed_tflops": performed / pms / 1e9, "fp64_dmma_peak_tflops": fp64_peak,
                  "frac_of_fp64_peak": performed / pms / 1e9 / fp64_peak}
-
-    # ---- warm-up ----
-    for _ in range(args.warmup):
-        step()
-    api.sync_status(sp)
 
     # ---- timed region: device-resident inputs ----
     api.set_timing(True)
