@@ -154,6 +154,22 @@ int rimp2_first_order(const int *nvirt, const int *nocc, const int *noccEOS, con
                       const double *UvirtT, const double *UoccT, const double *UoccallT,
                       const double *UvirtEOST, double *djik, double *blad);
 
+/* DEC fragment energies for general local orbitals, fused (no four-index
+ * array is formed).  With the inputs of rimp2_steps5to8 (RIMP2.F90:71-170):
+ *   Eocc  = sum toccEOS(aL,iL,bL,jL) (2 goccEOS(aL,iL,bL,jL) - goccEOS(bL,iL,aL,jL))
+ *   Evirt = sum tvirtEOS(aL,iL,bL,jL) (2 gvirtEOS(aL,iL,bL,jL) - gvirtEOS(aL,jL,bL,iL))
+ * (occupied and virtual partitioning of the fragment energy).  Both equal
+ *   sum_ij,ab g_ij^ab / D_ij^ab (2 gt_ij^ab - gt_ij^ba)
+ * where gt is the alpha contraction of Calpha projected on both orbital
+ * indices: Ct(:,a,i) = sum_ck Pv(a,c) Calpha(:,c,k) Po(k,i) with
+ * Po = UoccEOST UoccEOST^T, Pv = UvirtT UvirtT^T (occupied partitioning) or
+ * Po = UoccT UoccT^T, Pv = UvirtEOST UvirtEOST^T (virtual partitioning).
+ * With U = I both are the canonical MP2 energy.  FP64 on the GPU. */
+int rimp2_energy_eos(const int *nvirt, const int *nocc, const int *noccEOS, const int *nvirtEOS,
+                     const int *NBA, const double *Calpha, const double *EVocc,
+                     const double *EVvirt, const double *UoccEOST, const double *UvirtT,
+                     const double *UoccT, const double *UvirtEOST, double *Eocc, double *Evirt);
+
 /* ---- Calpha{1,2}.data files (host only) -----------------------------------
  * The reference's fragment files: Fortran unformatted sequential records
  * with 4-byte length markers, read by RIMP2.F90:36-63,190,229,257-360 and

@@ -194,6 +194,18 @@ def first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, Calpha, CalphaOcc,
     return djik, blad
 
 
+def energy_eos_from_arrays(toccEOS, goccEOS, tvirtEOS, gvirtEOS):
+    """Fragment energies from the reference's Step 5-8 arrays (restated MP2
+    expression in the local basis; the reference computes no energy):
+    Eocc = sum toccEOS(aL,iL,bL,jL) (2 goccEOS(aL,iL,bL,jL) - goccEOS(bL,iL,aL,jL)),
+    Evirt = sum tvirtEOS(aL,iL,bL,jL) (2 gvirtEOS(aL,iL,bL,jL) - gvirtEOS(aL,jL,bL,iL)).
+    Compensated (fsum) over all elements."""
+    import math
+    xo = toccEOS * (2.0 * goccEOS - np.transpose(goccEOS, (2, 1, 0, 3)))
+    xv = tvirtEOS * (2.0 * gvirtEOS - np.transpose(gvirtEOS, (0, 3, 2, 1)))
+    return math.fsum(xo.ravel()), math.fsum(xv.ravel())
+
+
 def _pairs_arg(pairs):
     if pairs is None:
         return None, 0, None

@@ -146,6 +146,20 @@ def first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, Calpha, CalphaOcc,
     return djik, blad
 
 
+def energy_eos(nvirt, nocc, noccEOS, nvirtEOS, NBA, Calpha, EVocc, EVvirt, UoccEOST, UvirtT,
+               UoccT, UvirtEOST):
+    """Fused DEC fragment energies (Eocc, Evirt) for general local orbitals
+    from the inputs of Steps 5-8 (C-ABI rimp2_energy_eos)."""
+    eo_ = C.c_double()
+    ev_ = C.c_double()
+    call("rimp2_energy_eos", _i(nvirt), _i(nocc), _i(noccEOS), _i(nvirtEOS), _i(NBA),
+         _a(Calpha, "Calpha", (NBA, nvirt, nocc)), _a(EVocc, "EVocc", (nocc,)),
+         _a(EVvirt, "EVvirt", (nvirt,)), _a(UoccEOST, "UoccEOST", (nocc, noccEOS)),
+         _a(UvirtT, "UvirtT", (nvirt, nvirt)), _a(UoccT, "UoccT", (nocc, nocc)),
+         _a(UvirtEOST, "UvirtEOST", (nvirt, nvirtEOS)), C.pointer(eo_), C.pointer(ev_))
+    return eo_.value, ev_.value
+
+
 DATAFILE_RECORDS = ("Calpha", "EVocc", "EVvirt", "UoccEOST", "UvirtT", "UoccT", "UvirtEOST",
                     "CalphaOcc", "CalphaVV", "toccEOS", "tvirtEOS", "gvirtEOS", "goccEOS",
                     "djik", "blad")

@@ -754,6 +754,60 @@ int rimp2_first_order(const int *nvirt_, const int *nocc_, const int *noccEOS_,
   return finish(s);
 }
 
+int rimp2_energy_eos(const int *nvirt_, const int *nocc_, const int *noccEOS_,
+                     const int *nvirtEOS_, const int *NBA_, const double *Calpha,
+                     const double *EVocc, const double *EVvirt, const double *UoccEOST,
+                     const double *UvirtT, const double *UoccT, const double *UvirtEOST,
+                     double *Eocc, double *Evirt) {
+  clear_error();
+  RIMP2_REQ(pos(nvirt_) && pos(nocc_) && pos(noccEOS_) && pos(nvirtEOS_) && pos(NBA_),
+            "rimp2_energy_eos: bad dims");
+  RIMP2_REQ(Calpha && EVocc && EVvirt && UoccEOST && UvirtT && UoccT && UvirtEOST && Eocc && Evirt,
+            "rimp2_energy_eos: null array");
+  RIMP2_TRY(ensure_device());
+  cudaStream_t s = current_stream();
+  const int nvirt = *nvirt_, nocc = *nocc_, noccEOS = *noccEOS_, nvirtEOS = *nvirtEOS_,
+            NBA = *NBA_;
+  const size_t nv = nvirt, no = nocc, ne = noccEOS, ve = nvirtEOS, nb = NBA;
+  DevBuf dC, deo, dev, dUoE, dUvT, dUoT, dUvE, Po, Pv, C2, Ct, Ep, Et;
+  RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
+  RIMP2_TRY(h2d(deo, EVocc, no, s));
+  RIMP2_TRY(h2d(dev, EVvirt, nv, s));
+  RIMP2_TRY(h2d(dUoE, UoccEOST, no * ne, s));
+  RIMP2_TRY(h2d(dUvT, UvirtT, nv * nv, s));
+  RIMP2_TRY(h2d(dUoT, UoccT, no * no, s));
+  RIMP2_TRY(h2d(dUvE, UvirtEOST, nv * ve, s));
+  RIMP2_TRY(dalloc(Po, no * no, s));
+  RIMP2_TRY(dalloc(Pv, nv * nv, s));
+  RIMP2_TRY(dalloc(C2, nb * nv * no, s));
+  RIMP2_TRY(dalloc(Ct, nb * nv * no, s));
+  RIMP2_TRY(dalloc(Ep, no * no, s));
+  RIMP2_TRY(dalloc(Et, 2, s));
+  const double *Uo[2] = {dUoE.as<double>(), dUoT.as<double>()};
+  const double *Uv[2] = {dUvT.as<double>(), dUvE.as<double>()};
+  const int ko[2] = {noccEOS, nocc}, kv[2] = {nvirt, nvirtEOS};
+  for (int part = 0; part < 2; ++part) {
+    // projectors Po = Uo Uo^T, Pv = Uv Uv^T
+    RIMP2_TRY(dev_dgemm('N', 'T', nocc, nocc, ko[part], 1.0, Uo[part], nocc, Uo[part], nocc, 0.0,
+                        Po.as<double>(), nocc, s));
+    RIMP2_TRY(dev_dgemm('N', 'T', nvirt, nvirt, kv[part], 1.0, Uv[part], nvirt, Uv[part], nvirt,
+                        0.0, Pv.as<double>(), nvirt, s));
+    // Ct(:,a,i) = sum_c Pv(c,a) sum_k Calpha(:,c,k) Po(k,i)
+    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nvirt, nocc, nocc, 1.0, dC.as<double>(), NBA * nvirt,
+                        Po.as<double>(), nocc, 0.0, C2.as<double>(), NBA * nvirt, s));
+    RIMP2_TRY(dev_transalpha2(nocc, nvirt, nvirt, NBA, Pv.as<double>(), C2.as<double>(),
+                              Ct.as<double>(), s));
+    RIMP2_TRY(eos_energy_f64(dC.as<double>(), Ct.as<double>(), NBA, nvirt, nocc, deo.as<double>(),
+                             dev.as<double>(), Ep.as<double>(), Et.as<double>() + part, s));
+  }
+  double h[2];
+  RIMP2_CK(cudaMemcpyAsync(h, Et.p, sizeof h, cudaMemcpyDeviceToHost, s));
+  RIMP2_TRY(finish(s));
+  *Eocc = h[0];
+  *Evirt = h[1];
+  return RIMP2_OK;
+}
+
 int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const double *dEVocc,
                      const double *dEVvirt, double *dEpair, double *dEtot, double *dtamp,
                      int precision, void *stream) {

@@ -104,6 +104,10 @@ int probe_fp64_peak(double *tflops, cudaStream_t s);
 void plain_energy_scratch_sizes(int nvirt, int nocc, long long *npairs, long long *nitems);
 int plain_energy_f64_scratch(const PlainEnergyArgs &a, int *pairs_scratch, double *part_scratch,
                              cudaStream_t s);
+// Fused local-orbital energy from Calpha and its projected copy Ct (FP64).
+int eos_energy_f64(const double *Ca, const double *Ct, int NBA, int nvirt, int nocc,
+                   const double *eo, const double *ev, double *Epair, double *Etot,
+                   cudaStream_t s);
 // Batched plain FP64 energies: every fragment's (pair, 64x64 tile pair) items
 // in one persistent launch, then per-fragment compensated reductions.
 struct PlainFrag {

@@ -150,24 +150,21 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Energy contribution of tile pair (tA,tB) of occupied pair (i<=j); the
-// block sum is valid in thread 0.  Shared staging P and red are the caller's.
-__device__ __forceinline__ double plain_tile_pair(double (&P)[4][TM][KP], double *red,
-                                                  const double *__restrict__ Ca, int NBA,
-                                                  int nvirt, int nocc,
-                                                  const double *__restrict__ eo,
-                                                  const double *__restrict__ ev, int i, int j,
-                                                  int tA, int tB, double *__restrict__ tamp) {
+// Accumulate T1 = C_iA^T C_jB and T2 = C_jA^T C_iB (64x64 each, FP64 DMMA)
+// over the whole K = NBA for the tile pair at (a0, b0); i = j skips T2.
+// Fragment ownership: warp w holds rows wm + 8x + gid, columns wn + 8y + 2 tig + h.
+__device__ __forceinline__ void accumulate_tile_pair(double (&P)[4][TM][KP],
+                                                     const double *__restrict__ Ca, int NBA,
+                                                     int nvirt, int i, int j, int a0, int b0,
+                                                     double (&t1)[4][2][2],
+                                                     double (&t2)[4][2][2]) {
   const bool same = (i == j);
-  const int a0 = tA * TM, b0 = tB * TN;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
   const int gid = lane >> 2, tig = lane & 3;
   const size_t colstride = (size_t)NBA;
   const double *ci = Ca + (size_t)NBA * nvirt * i;
   const double *cj = Ca + (size_t)NBA * nvirt * j;
-
-  double t1[4][2][2], t2[4][2][2];
 #pragma unroll
   for (int x = 0; x < 4; ++x)
 #pragma unroll
@@ -214,6 +211,25 @@ __device__ __forceinline__ double plain_tile_pair(double (&P)[4][TM][KP], double
     }
     __syncthreads();
   }
+
+}
+
+// Energy contribution of tile pair (tA,tB) of occupied pair (i<=j); the
+// block sum is valid in thread 0.  Shared staging P and red are the caller's.
+__device__ __forceinline__ double plain_tile_pair(double (&P)[4][TM][KP], double *red,
+                                                  const double *__restrict__ Ca, int NBA,
+                                                  int nvirt, int nocc,
+                                                  const double *__restrict__ eo,
+                                                  const double *__restrict__ ev, int i, int j,
+                                                  int tA, int tB, double *__restrict__ tamp) {
+  const bool same = (i == j);
+  const int a0 = tA * TM, b0 = tB * TN;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
+  const int gid = lane >> 2, tig = lane & 3;
+
+  double t1[4][2][2], t2[4][2][2];
+  accumulate_tile_pair(P, Ca, NBA, nvirt, i, j, a0, b0, t1, t2);
 
   // epilogue: denominators, amplitudes, energy contribution
   const double eij = eo[i] + eo[j];
@@ -274,6 +290,82 @@ __global__ void __launch_bounds__(NTHR, 2) plain_energy_kernel(const double *__r
   const double s = plain_tile_pair(P, red, Ca, NBA, nvirt, nocc, eo, ev, pairs[2 * p],
                                    pairs[2 * p + 1], tA, tB, tamp);
   if (threadIdx.x == 0) part[item] = s;
+}
+
+// Fragment energy with local orbitals, fused: for Calpha C and its projected
+// copy Ct (both (NBA,nvirt,nocc)), tile pair (tA,tB) of pair (i<=j) adds
+//   sum_(a,b) g_ij^ab / D * (2 gt_ij^ab - gt_ij^ba)
+// over (a in A, b in B) and, off the diagonal tile pair, (a in B, b in A),
+// where g comes from C and gt from Ct.  T1/T2 of C are accumulated first and
+// parked in a thread-private shared-memory stash (each thread reads back only
+// what it wrote), then T1/T2 of Ct; registers stay at the plain kernel's.
+constexpr int EOS_STASH = 32;  // doubles per thread
+constexpr int EOS_SMEM = (4 * TM * KP + EOS_STASH * NTHR + NTHR / 32) * (int)sizeof(double);
+
+__global__ void __launch_bounds__(NTHR, 2) eos_energy_kernel(const double *__restrict__ Ca,
+                                                             const double *__restrict__ Ct,
+                                                             int NBA, int nvirt,
+                                                             const double *__restrict__ eo,
+                                                             const double *__restrict__ ev,
+                                                             const int *__restrict__ pairs,
+                                                             int ntile, double *__restrict__ part) {
+  extern __shared__ double esm[];
+  double(&P)[4][TM][KP] = *reinterpret_cast<double(*)[4][TM][KP]>(esm);
+  double *stash = esm + 4 * TM * KP;          // [EOS_STASH][NTHR]
+  double *red = stash + EOS_STASH * NTHR;     // [NTHR / 32]
+  const int ntp = ntile * (ntile + 1) / 2;
+  const long long item = blockIdx.x;
+  const int p = (int)(item / ntp), q = (int)(item % ntp);
+  int tA, tB;
+  decode_tri(q, tA, tB);
+  const int i = pairs[2 * p], j = pairs[2 * p + 1];
+  const bool same = (i == j), diag = (tA == tB);
+  const int a0 = tA * TM, b0 = tB * TN;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
+  const int gid = lane >> 2, tig = lane & 3;
+
+  double t1[4][2][2], t2[4][2][2];
+  accumulate_tile_pair(P, Ca, NBA, nvirt, i, j, a0, b0, t1, t2);
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 2; ++y)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = (x * 2 + y) * 2 + h;
+        stash[(2 * r) * NTHR + tid] = t1[x][y][h];
+        stash[(2 * r + 1) * NTHR + tid] = same ? t1[x][y][h] : t2[x][y][h];
+      }
+  accumulate_tile_pair(P, Ct, NBA, nvirt, i, j, a0, b0, t1, t2);  // now gt
+
+  const double eij = eo[i] + eo[j];
+  double e = 0.0;
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 2; ++y)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int a = a0 + wm + 8 * x + gid;
+        const int b = b0 + wn + 8 * y + 2 * tig + h;
+        if (a < nvirt && b < nvirt) {
+          const int r = (x * 2 + y) * 2 + h;
+          const double g1 = stash[(2 * r) * NTHR + tid], g2 = stash[(2 * r + 1) * NTHR + tid];
+          const double u1 = t1[x][y][h], u2 = same ? u1 : t2[x][y][h];
+          const double d = eij - ev[b] - ev[a];  // RIMP2.F90:403 order
+          e += g1 / d * (2.0 * u1 - u2);
+          if (!diag) e += g2 / d * (2.0 * u2 - u1);
+        }
+      }
+  e = warp_sum(e);
+  if (lane == 0) red[warp] = e;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NTHR / 32; ++w) s += red[w];
+    part[item] = s;
+  }
 }
 
 // Batched form: one persistent launch drains a queue of (fragment, pair,
@@ -584,6 +676,42 @@ int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s) {
   return RIMP2_OK;
 }
 
+
+// Fused local-orbital fragment energy: Epair(i,j) = sum_ab g_ij^ab/D (2 gt_ij^ab
+// - gt_ij^ba) from Calpha and its projected copy Ct; Etot = sum_ij Epair.
+int eos_energy_f64(const double *Ca, const double *Ct, int NBA, int nvirt, int nocc,
+                   const double *eo, const double *ev, double *Epair, double *Etot,
+                   cudaStream_t s) {
+  static_assert(EOS_SMEM <= 227 * 1024, "EOS kernel shared memory");
+  const int ntile = (nvirt + TM - 1) / TM;
+  const int ntp = ntile * (ntile + 1) / 2;
+  const int npairs = nocc * (nocc + 1) / 2;
+  const long long nitems = (long long)npairs * ntp;
+  if (nitems > 2147483647LL) {
+    set_error("too many work items (%lld)", nitems);
+    return RIMP2_ERR_ARG;
+  }
+  RIMP2_CK(cudaFuncSetAttribute(eos_energy_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                EOS_SMEM));
+  DevBuf pairs, part;
+  RIMP2_TRY(pairs.alloc(sizeof(int) * 2 * (size_t)npairs, s));
+  RIMP2_TRY(part.alloc(sizeof(double) * (size_t)nitems, s));
+  if (inject_fault("launch")) {
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  make_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(nocc, pairs.as<int>());
+  RIMP2_CK(cudaMemsetAsync(Epair, 0, sizeof(double) * (size_t)nocc * nocc, s));
+  eos_energy_kernel<<<(unsigned)nitems, NTHR, EOS_SMEM, s>>>(Ca, Ct, NBA, nvirt, eo, ev,
+                                                              pairs.as<int>(), ntile,
+                                                              part.as<double>());
+  pair_reduce_kernel<<<(npairs + 7) / 8, 256, 0, s>>>(part.as<double>(), ntp, pairs.as<int>(),
+                                                     npairs, nocc, Epair);
+  total_reduce_kernel<<<1, 1024, 0, s>>>(Epair, nocc, Etot);
+  count_launch(4);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
 
 // A planned plain FP64 batch: fragment table, per-item partials, queue.
 struct PlainPlan {

@@ -128,6 +128,18 @@ module rimp2_gpu_interfaces
        real(C_DOUBLE), intent(inout) :: gvirtEOS(nvirtEOS,nocc,nvirtEOS,nocc)
      end function rimp2_steps5to8
 
+     ! fused fragment energies (occupied and virtual partitioning) for general U
+     integer(C_INT) function rimp2_energy_eos(nvirt, nocc, noccEOS, nvirtEOS, NBA, Calpha, EVocc, &
+          & EVvirt, UoccEOST, UvirtT, UoccT, UvirtEOST, Eocc, Evirt) &
+          & bind(C, name="rimp2_energy_eos")
+       import :: C_INT, C_DOUBLE
+       integer(C_INT), intent(in) :: nvirt, nocc, noccEOS, nvirtEOS, NBA
+       real(C_DOUBLE), intent(in) :: Calpha(NBA,nvirt,nocc), EVocc(nocc), EVvirt(nvirt)
+       real(C_DOUBLE), intent(in) :: UoccEOST(nocc,noccEOS), UvirtT(nvirt,nvirt)
+       real(C_DOUBLE), intent(in) :: UoccT(nocc,nocc), UvirtEOST(nvirt,nvirtEOS)
+       real(C_DOUBLE), intent(out) :: Eocc, Evirt
+     end function rimp2_energy_eos
+
      ! first-order block of the driver (RIMP2.F90:172-251); pass UoccT as UoccallT
      integer(C_INT) function rimp2_first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, &
           & Calpha, CalphaOcc, CalphaVV, UoccEOST, UvirtT, UoccT, UoccallT, UvirtEOST, djik, blad) &

@@ -193,6 +193,42 @@ def test_first_order_rejects_nocc_above_nvirt(api):
     assert ei.value.status == 1
 
 
+def test_energy_eos_golden_general(api, golden):
+    """Fused local-orbital fragment energies against the energies contracted
+    from the reference's own Step 5-8 arrays (random non-unitary U)."""
+    g = golden("small_general.npz")
+    n = {k: int(g[k]) for k in ("nvirt", "nocc", "noccEOS", "nvirtEOS", "NBA")}
+    A = [np.asfortranarray(g[k]) for k in ("Calpha", "EVocc", "EVvirt", "UoccEOST", "UvirtT",
+                                           "UoccT", "UvirtEOST")]
+    eocc, evir = api.energy_eos(n["nvirt"], n["nocc"], n["noccEOS"], n["nvirtEOS"], n["NBA"], *A)
+    ro, rv = O.energy_eos_from_arrays(g["toccEOS"], g["goccEOS"], g["tvirtEOS"], g["gvirtEOS"])
+    assert abs(eocc - ro) <= 1e-11 * abs(ro), (eocc, ro)
+    assert abs(evir - rv) <= 1e-11 * abs(rv), (evir, rv)
+
+
+def test_energy_eos_fragment_vs_oracle_arrays(api):
+    """nocc=16, nvirt=96, NBA=384 with orthonormal local-orbital blocks
+    (noccEOS=5, nvirtEOS=24): oracle Steps 5-8 arrays contracted in FP64."""
+    nocc, nvirt, NBA, noE, nvE = 16, 96, 384, 5, 24
+    Ca, eo, ev = O.gen_fragment(21, nocc, nvirt, NBA)
+    q = lambda m, k, s: np.asfortranarray(np.linalg.qr(O.gen_matrix(21, s, m, m))[0][:, :k])  # noqa
+    UoE, UvT, UoT, UvE = q(nocc, noE, 30), q(nvirt, nvirt, 31), q(nocc, nocc, 32), q(nvirt, nvE, 33)
+    tE, vE, gE, gvE = O.steps5to8(nvirt, nocc, noE, nvE, NBA, Ca, eo, ev, UoE, UvT, UoT, UvE)
+    ro, rv = O.energy_eos_from_arrays(tE, gE, vE, gvE)
+    eocc, evir = api.energy_eos(nvirt, nocc, noE, nvE, NBA, Ca, eo, ev, UoE, UvT, UoT, UvE)
+    assert abs(eocc - ro) <= 1e-11 * abs(ro), (eocc, ro)
+    assert abs(evir - rv) <= 1e-11 * abs(rv), (evir, rv)
+
+
+def test_energy_eos_identity_is_canonical(api):
+    nocc, nvirt, NBA = 7, 65, 129
+    Ca, eo, ev = O.gen_fragment(22, nocc, nvirt, NBA)
+    Io, Iv = np.eye(nocc, order="F"), np.eye(nvirt, order="F")
+    eocc, evir = api.energy_eos(nvirt, nocc, nocc, nvirt, NBA, Ca, eo, ev, Io, Iv, Io, Iv)
+    _, E = api.energy(nvirt, nocc, NBA, Ca, eo, ev)
+    assert abs(eocc - E) <= 1e-12 * abs(E) and abs(evir - E) <= 1e-12 * abs(E)
+
+
 def test_get_dev_mem(api):
     total, free = api.get_dev_mem()
     assert total > 200e9 and 0 < free <= total

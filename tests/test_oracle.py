@@ -159,6 +159,33 @@ def test_energy_from_reference_arrays_identity():
     assert abs(e_vir - E) <= 1e-13 * abs(E)
 
 
+def fused_eos_numpy(Ca, eo, ev, Uo, Uv):
+    """sum_ij,ab g_ij^ab/D (2 gt_ij^ab - gt_ij^ba) with gt from Calpha
+    projected by Po = Uo Uo^T and Pv = Uv Uv^T (plain numpy)."""
+    Po, Pv = Uo @ Uo.T, Uv @ Uv.T
+    Ct = np.einsum("ac,xck,ki->xai", Pv, Ca, Po)
+    g = np.einsum("xai,xbj->iajb", Ca, Ca)
+    gt = np.einsum("xai,xbj->iajb", Ct, Ct)
+    D = eo[:, None, None, None] + eo[None, None, :, None] - ev[None, :, None, None] - \
+        ev[None, None, None, :]
+    return float(np.sum(g / D * (2 * gt - gt.transpose(0, 3, 2, 1))))
+
+
+def test_fused_eos_energy_equals_reference_arrays(golden):
+    """The fused local-orbital energy (projected Calpha) equals the energy
+    contracted from the reference's own Step 5-8 arrays, for random
+    non-unitary U (golden case): both partitionings."""
+    g = golden("small_general.npz")
+    A = {k: np.asarray(g[k]) for k in ("Calpha", "EVocc", "EVvirt", "UoccEOST", "UvirtT", "UoccT",
+                                       "UvirtEOST")}
+    e_occ, e_vir = O.energy_eos_from_arrays(g["toccEOS"], g["goccEOS"], g["tvirtEOS"],
+                                            g["gvirtEOS"])
+    f_occ = fused_eos_numpy(A["Calpha"], A["EVocc"], A["EVvirt"], A["UoccEOST"], A["UvirtT"])
+    f_vir = fused_eos_numpy(A["Calpha"], A["EVocc"], A["EVvirt"], A["UoccT"], A["UvirtEOST"])
+    assert abs(f_occ - e_occ) <= 1e-12 * abs(e_occ)
+    assert abs(f_vir - e_vir) <= 1e-12 * abs(e_vir)
+
+
 def test_amplitudes_match_tocca_with_identity():
     nvirt, nocc, NBA = 9, 3, 17
     Ca, eo, ev = O.gen_fragment(7, nocc, nvirt, NBA)
