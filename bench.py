@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--workload", choices=["fragment", "batched", "ao"], default="fragment",
                     help="fragment: one nocc=128/nvirt=1024/NBA=4096 fragment (default); "
                          "batched: 256 uneven fragments in one graph-launched persistent kernel")
+    ap.add_argument("--batch-fragments", type=int, default=256,
+                    help="batched workload: the first N of the 256 seeded shapes (profiling)")
     ap.add_argument("--ao-fragments", type=int, default=AO_N_DEFAULT,
                     help="fragments in the AO pipeline workload")
     ap.add_argument("--ao-transform", choices=["split", "fp64"], default="split",
@@ -517,7 +519,7 @@ def run_batched(args):
     dev = torch.device("cuda", local)
     st = torch.cuda.Stream(device=dev)
     sp = st.cuda_stream
-    shapes = batch_shapes()
+    shapes = batch_shapes()[:args.batch_fragments]
     eff = sum(2.0 * b * (o * v) ** 2 for o, v, b in shapes)
     frags, desc = [], []
     with torch.cuda.stream(st):

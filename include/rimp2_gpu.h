@@ -164,11 +164,15 @@ int rimp2_first_order(const int *nvirt, const int *nocc, const int *noccEOS, con
  * indices: Ct(:,a,i) = sum_ck Pv(a,c) Calpha(:,c,k) Po(k,i) with
  * Po = UoccEOST UoccEOST^T, Pv = UvirtT UvirtT^T (occupied partitioning) or
  * Po = UoccT UoccT^T, Pv = UvirtEOST UvirtEOST^T (virtual partitioning).
- * With U = I both are the canonical MP2 energy.  FP64 on the GPU. */
+ * With U = I both are the canonical MP2 energy.  precision: RIMP2_PREC_FP64
+ * (FP64 DMMA) or RIMP2_PREC_SPLIT (tcgen05 split form with the slice count of
+ * the shape-bucket table; relative error within 1e-7).  Ct is formed with
+ * FP64 GEMMs either way. */
 int rimp2_energy_eos(const int *nvirt, const int *nocc, const int *noccEOS, const int *nvirtEOS,
                      const int *NBA, const double *Calpha, const double *EVocc,
                      const double *EVvirt, const double *UoccEOST, const double *UvirtT,
-                     const double *UoccT, const double *UvirtEOST, double *Eocc, double *Evirt);
+                     const double *UoccT, const double *UvirtEOST, double *Eocc, double *Evirt,
+                     const int *precision);
 
 /* ---- Calpha{1,2}.data files (host only) -----------------------------------
  * The reference's fragment files: Fortran unformatted sequential records

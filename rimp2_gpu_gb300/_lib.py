@@ -45,7 +45,7 @@ SIGNATURES = {
                      _ip], C.c_int),
     "rimp2_steps5to8": ([_ip] * 5 + [_dp] * 11, C.c_int),
     "rimp2_first_order": ([_ip] * 6 + [_dp] * 10, C.c_int),
-    "rimp2_energy_eos": ([_ip] * 5 + [_dp] * 9, C.c_int),
+    "rimp2_energy_eos": ([_ip] * 5 + [_dp] * 9 + [_ip], C.c_int),
     "rimp2_datafile_header": ([C.c_char_p, _ip], C.c_int),
     "rimp2_datafile_read": ([C.c_char_p, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
     "rimp2_datafile_write": ([C.c_char_p, _ip, C.c_int, C.POINTER(C.c_void_p)], C.c_int),

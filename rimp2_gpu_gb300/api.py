@@ -147,16 +147,17 @@ def first_order(nvirt, nocc, noccEOS, nvirtEOS, nocctot, NBA, Calpha, CalphaOcc,
 
 
 def energy_eos(nvirt, nocc, noccEOS, nvirtEOS, NBA, Calpha, EVocc, EVvirt, UoccEOST, UvirtT,
-               UoccT, UvirtEOST):
+               UoccT, UvirtEOST, precision=PREC_FP64):
     """Fused DEC fragment energies (Eocc, Evirt) for general local orbitals
-    from the inputs of Steps 5-8 (C-ABI rimp2_energy_eos)."""
+    from the inputs of Steps 5-8 (C-ABI rimp2_energy_eos); FP64 or split."""
     eo_ = C.c_double()
     ev_ = C.c_double()
     call("rimp2_energy_eos", _i(nvirt), _i(nocc), _i(noccEOS), _i(nvirtEOS), _i(NBA),
          _a(Calpha, "Calpha", (NBA, nvirt, nocc)), _a(EVocc, "EVocc", (nocc,)),
          _a(EVvirt, "EVvirt", (nvirt,)), _a(UoccEOST, "UoccEOST", (nocc, noccEOS)),
          _a(UvirtT, "UvirtT", (nvirt, nvirt)), _a(UoccT, "UoccT", (nocc, nocc)),
-         _a(UvirtEOST, "UvirtEOST", (nvirt, nvirtEOS)), C.pointer(eo_), C.pointer(ev_))
+         _a(UvirtEOST, "UvirtEOST", (nvirt, nvirtEOS)), C.pointer(eo_), C.pointer(ev_),
+         _i(precision))
     return eo_.value, ev_.value
 
 

@@ -758,12 +758,15 @@ int rimp2_energy_eos(const int *nvirt_, const int *nocc_, const int *noccEOS_,
                      const int *nvirtEOS_, const int *NBA_, const double *Calpha,
                      const double *EVocc, const double *EVvirt, const double *UoccEOST,
                      const double *UvirtT, const double *UoccT, const double *UvirtEOST,
-                     double *Eocc, double *Evirt) {
+                     double *Eocc, double *Evirt, const int *precision) {
   clear_error();
   RIMP2_REQ(pos(nvirt_) && pos(nocc_) && pos(noccEOS_) && pos(nvirtEOS_) && pos(NBA_),
             "rimp2_energy_eos: bad dims");
-  RIMP2_REQ(Calpha && EVocc && EVvirt && UoccEOST && UvirtT && UoccT && UvirtEOST && Eocc && Evirt,
+  RIMP2_REQ(Calpha && EVocc && EVvirt && UoccEOST && UvirtT && UoccT && UvirtEOST && Eocc &&
+                Evirt && precision,
             "rimp2_energy_eos: null array");
+  RIMP2_REQ(*precision == RIMP2_PREC_FP64 || *precision == RIMP2_PREC_SPLIT,
+            "rimp2_energy_eos: precision must be 0 (FP64) or 1 (split)");
   RIMP2_TRY(ensure_device());
   cudaStream_t s = current_stream();
   const int nvirt = *nvirt_, nocc = *nocc_, noccEOS = *noccEOS_, nvirtEOS = *nvirtEOS_,
@@ -797,8 +800,14 @@ int rimp2_energy_eos(const int *nvirt_, const int *nocc_, const int *noccEOS_,
                         Po.as<double>(), nocc, 0.0, C2.as<double>(), NBA * nvirt, s));
     RIMP2_TRY(dev_transalpha2(nocc, nvirt, nvirt, NBA, Pv.as<double>(), C2.as<double>(),
                               Ct.as<double>(), s));
-    RIMP2_TRY(eos_energy_f64(dC.as<double>(), Ct.as<double>(), NBA, nvirt, nocc, deo.as<double>(),
-                             dev.as<double>(), Ep.as<double>(), Et.as<double>() + part, s));
+    if (*precision == RIMP2_PREC_SPLIT)
+      RIMP2_TRY(split_eos_energy(dC.as<double>(), Ct.as<double>(), NBA, nvirt, nocc,
+                                 deo.as<double>(), dev.as<double>(), Ep.as<double>(),
+                                 Et.as<double>() + part, rimp2_split_nslices(nvirt, nocc, NBA), s));
+    else
+      RIMP2_TRY(eos_energy_f64(dC.as<double>(), Ct.as<double>(), NBA, nvirt, nocc,
+                               deo.as<double>(), dev.as<double>(), Ep.as<double>(),
+                               Et.as<double>() + part, s));
   }
   double h[2];
   RIMP2_CK(cudaMemcpyAsync(h, Et.p, sizeof h, cudaMemcpyDeviceToHost, s));

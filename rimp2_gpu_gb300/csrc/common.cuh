@@ -132,6 +132,10 @@ struct SplitEnergyArgs {
   int nslices;  // residual slices per element (1 or 2)
 };
 int split_energy(const SplitEnergyArgs &a, cudaStream_t s, float *ms_kernel);
+// local-orbital fragment energy (Calpha and its projected copy Ct), split form
+int split_eos_energy(const double *Ca, const double *Ct, int NBA, int nvirt, int nocc,
+                     const double *eo, const double *ev, double *Epair, double *Etot,
+                     int nslices, cudaStream_t s);
 struct SplitPlan;
 int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nvirt, const int *NBA,
                       const double *const *Ca, const double *const *eo, const double *const *ev,

@@ -733,6 +733,354 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   }
 }
 
+// ==========================================================================
+// Local-orbital fragment energy on the tensor cores (split form):
+//   sum_ij,ab g_ij^ab / D (2 gt_ij^ab - gt_ij^ba),
+// g from Calpha C, gt from its projected copy Ct (both sliced like Calpha).
+// Work item = (pair i<=j, tile pair A<=B, column half h): rows a in block A
+// (128), columns b in the h-th 64-column half of block B.  Four 128x64 tiles
+// per item: T1 = C_iA^T C_jB, T2 = C_jA^T C_iB, U1 = Ct_iA^T Ct_jB,
+// U2 = Ct_jA^T Ct_iB, each with L0/L1 accumulators: 8 x 64 = 512 TMEM columns.
+// Diagonal tile pairs compute T2/U2 too (no transpose), so each ordered (a,b)
+// of A x A is met once over the two halves; i = j reuses T1/U1.
+// Roles as in split_batch_kernel; the MMA issuer waits for the epilogue to
+// free all four tiles before the next item (no accumulator double-buffer).
+// --------------------------------------------------------------------------
+constexpr int HALF = 64;
+constexpr int HPANEL_BYTES = HALF * KSTEP * 2;  // 8 KB
+
+struct EosParams {
+  const float *inv;          // inverse scales: C columns [0, ncol), Ct columns [ncol, 2 ncol)
+  const float2 *eo2, *ev2;   // hi/lo orbital energies (ev2 padded to nvpad)
+  long long nitems;
+  unsigned int *queue;
+  double *part;              // [nitems]
+  int *err;
+  int nocc, nvirt, nvpad, nks, ntp, ncol;
+  int rowC, rowCt;           // first slice row of C and of Ct (per plane)
+};
+
+__device__ __forceinline__ void eos_decode(const EosParams &P, long long id, int &i, int &j,
+                                           int &tA, int &tB, int &h) {
+  const int per = 2 * P.ntp;
+  const int p = (int)(id / per), r = (int)(id % per);
+  decode_pair(p, i, j);
+  decode_tri(r >> 1, tA, tB);
+  h = r & 1;
+}
+
+template <int NSL, int NSTAGE>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    split_eos_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     EosParams P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int STAGE_BYTES = NSL * (PANEL_BYTES + HPANEL_BYTES);
+  constexpr int NEPI = 8;
+  uint8_t *stages = base;
+  uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
+  // bars: full[NSTAGE], empty[NSTAGE], accfull, accempty, drain, item_full[IQ],
+  //       item_empty[IQ]
+  constexpr int NB = 2 * NSTAGE + 3 + 2 * IQ;
+  uint32_t *tmem_slot = (uint32_t *)(bars + NB);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  volatile long long *item_q =
+      (volatile long long *)(((uintptr_t)(tmem_slot + 2) + 7) & ~(uintptr_t)7);  // [IQ]
+  double *redd = (double *)(item_q + IQ);                                       // [NEPI]
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t full0 = smem_u32(&bars[0]);
+  const uint32_t empty0 = smem_u32(&bars[NSTAGE]);
+  const uint32_t accfull = smem_u32(&bars[2 * NSTAGE]);
+  const uint32_t accempty = smem_u32(&bars[2 * NSTAGE + 1]);
+  const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 2]);
+  const uint32_t ifull0 = smem_u32(&bars[2 * NSTAGE + 3]);
+  const uint32_t iempty0 = smem_u32(&bars[2 * NSTAGE + 3 + IQ]);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(accfull, 1);
+    mbar_init(accempty, NEPI);
+    mbar_init(drain, 1);
+    for (int s = 0; s < IQ; ++s) {
+      mbar_init(ifull0 + 8 * s, 1);
+      mbar_init(iempty0 + 8 * s, 1 + NEPI);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------ TMA producer ------------------------------
+    if (lane == 0) {
+      int stage = 0, islot = 0;
+      uint32_t phase = 0, iphase = 0;
+      int armed[NSTAGE];
+      for (int s = 0; s < NSTAGE; ++s) armed[s] = -1;
+      bool ok = true;
+      while (ok) {
+        if (!mbar_wait(iempty0 + 8 * islot, iphase ^ 1, abort_flag, P.err, 5)) break;
+        const long long id = (long long)atomicAdd(P.queue, 1u);
+        const long long qidx = id < P.nitems ? id : -1;
+        item_q[islot] = qidx;
+        mbar_arrive(ifull0 + 8 * islot);
+        if (++islot == IQ) {
+          islot = 0;
+          iphase ^= 1;
+        }
+        if (qidx < 0) break;
+        int i, j, tA, tB, h;
+        eos_decode(P, qidx, i, j, tA, tB, h);
+        const bool same = (i == j);
+        for (int t = 0; t < 4 && ok; ++t) {
+          if (same && (t & 1)) continue;  // T2 = T1, U2 = U1
+          const int rowbase = (t < 2) ? P.rowC : P.rowCt;
+          const int ia = (t & 1) ? j : i, ib = (t & 1) ? i : j;
+          const int colA = ia * P.nvpad + tA * TILE;
+          const int colB = ib * P.nvpad + tB * TILE + h * HALF;
+          for (int kc = 0; kc < P.nks; ++kc) {
+            if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err, 1)) {
+              ok = false;
+              break;
+            }
+            const uint32_t fb = full0 + 8 * stage;
+            mbar_expect_tx(fb, STAGE_BYTES);
+            armed[stage] = (int)phase;
+            const uint32_t dst = smem_u32(stages + stage * STAGE_BYTES);
+            const int rowk = rowbase + kc * P.ncol;
+#pragma unroll
+            for (int sl = 0; sl < NSL; ++sl) {
+              tma_load_3d(dst + sl * PANEL_BYTES, &tmA, fb, 0, rowk + colA, sl);
+              tma_load_3d(dst + NSL * PANEL_BYTES + sl * HPANEL_BYTES, &tmB, fb, 0, rowk + colB,
+                          sl);
+            }
+            if (++stage == NSTAGE) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+      }
+      if (!ok || *abort_flag) {  // drain copies in flight before the CTA can exit
+        for (int s = 0; s < NSTAGE; ++s) {
+          if (armed[s] < 0) continue;
+          const long long t0 = clock64();
+          while (!mbar_test(full0 + 8 * s, (uint32_t)armed[s]) && clock64() - t0 < WAIT_BUDGET) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------ MMA issuer --------------------------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = (IDESC & ~(0x3Fu << 17)) | ((uint32_t)(HALF >> 3) << 17);
+      int stage = 0, islot = 0;
+      uint32_t phase = 0, iphase = 0;
+      bool ok = true;
+      long long nloc = 0;
+      while (ok) {
+        if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 6)) break;
+        const long long qidx = item_q[islot];
+        mbar_arrive(iempty0 + 8 * islot);
+        if (++islot == IQ) {
+          islot = 0;
+          iphase ^= 1;
+        }
+        if (qidx < 0) break;
+        int i, j, tA, tB, h;
+        eos_decode(P, qidx, i, j, tA, tB, h);
+        const bool same = (i == j);
+        // the previous item's accumulators must have been read out
+        if (nloc > 0 &&
+            !mbar_wait(accempty, (uint32_t)((nloc - 1) & 1), abort_flag, P.err, 2)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        for (int t = 0; t < 4 && ok; ++t) {
+          if (same && (t & 1)) continue;
+          const uint32_t dL0 = tmem + (uint32_t)(t * 2 * HALF);
+          const uint32_t dL1 = dL0 + HALF;
+          for (int kc = 0; kc < P.nks; ++kc) {
+            if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err, 3)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sb = smem_u32(stages + stage * STAGE_BYTES);
+            const uint32_t sbB = sb + NSL * PANEL_BYTES;
+#pragma unroll
+            for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
+              const uint32_t koff = k16 * 32;
+              const uint64_t a0 = smem_desc(sb + 0 * PANEL_BYTES + koff);
+              const uint64_t a1 = smem_desc(sb + 1 * PANEL_BYTES + koff);
+              const uint64_t b0 = smem_desc(sbB + 0 * HPANEL_BYTES + koff);
+              const uint64_t b1 = smem_desc(sbB + 1 * HPANEL_BYTES + koff);
+              const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
+              mma_f16_id(dL0, a0, b0, idesc, acc);  // exact integer part
+              mma_f16_id(dL1, a0, b1, idesc, acc);  // S0a R1b
+              mma_f16_id(dL1, a1, b0, idesc, 1u);   // R1a S0b
+              mma_f16_id(dL1, a1, b1, idesc, 1u);   // R1a R1b
+              if (NSL > 2) {
+                const uint64_t a2 = smem_desc(sb + 2 * PANEL_BYTES + koff);
+                const uint64_t b2 = smem_desc(sbB + 2 * HPANEL_BYTES + koff);
+                mma_f16_id(dL1, a0, b2, idesc, 1u);  // S0a R2b
+                mma_f16_id(dL1, a2, b0, idesc, 1u);  // R2a S0b
+              }
+            }
+            mma_commit(empty0 + 8 * stage);
+            if (++stage == NSTAGE) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+        if (!ok) break;
+        mma_commit(accfull);
+        ++nloc;
+      }
+      // drain: all MMAs issued by this thread complete before TMEM is freed
+      mma_commit(drain);
+      const long long t0 = clock64();
+      while (!mbar_test(drain, 0) && clock64() - t0 < WAIT_BUDGET) {
+      }
+    }
+  } else {
+    // ------------------------------ epilogue ----------------------------------
+    const int ew = warp - 2;             // 0..7
+    const int quad = warp & 3;
+    const int cbase = (ew >> 2) * 32;    // 32 of the tile's 64 columns
+    const int row = quad * 32 + lane;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    int islot = 0;
+    uint32_t iphase = 0;
+    long long nloc = 0;
+    while (true) {
+      if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7)) break;
+      const long long qidx = item_q[islot];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(iempty0 + 8 * islot);
+      if (++islot == IQ) {
+        islot = 0;
+        iphase ^= 1;
+      }
+      if (qidx < 0) break;
+      int i, j, tA, tB, h;
+      eos_decode(P, qidx, i, j, tA, tB, h);
+      const bool same = (i == j), diag = (tA == tB);
+      const int a = tA * TILE + row;
+      const int b0 = tB * TILE + h * HALF + cbase;
+      const float *sc = P.inv, *st = P.inv + P.ncol;
+      const float sCi = sc[i * P.nvpad + a], sCj = sc[j * P.nvpad + a];
+      const float sTi = st[i * P.nvpad + a], sTj = st[j * P.nvpad + a];
+      const float2 ea = P.ev2[a];
+      const float2 ei = P.eo2[i], ej = P.eo2[j];
+      const float sh = ei.x + ej.x;
+      const float bv = sh - ei.x;
+      const float sl = (ei.x - (sh - bv)) + (ej.x - bv) + ei.y + ej.y;
+      const float dh0 = sh - ea.x;
+      const float bw = dh0 - sh;
+      const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
+      if (!mbar_wait(accfull, (uint32_t)(nloc & 1), abort_flag, P.err, 4)) break;
+      tc_fence_after();
+      double eacc = 0.0;
+#pragma unroll 1
+      for (int c0 = 0; c0 < 32; c0 += 16) {
+        float g1[16], g2[16], u1[16], u2[16];
+        {
+          float l0[16], l1[16];
+          const uint32_t tt = tmem + lane_off + cbase + c0;
+          tmem_ld16(tt + 0 * HALF, l0);
+          tmem_ld16(tt + 1 * HALF, l1);
+          tmem_wait_ld();
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            g1[k] = (l0[k] + l1[k]) * (sCi * sc[j * P.nvpad + b0 + c0 + k]);
+          tmem_ld16(tt + 4 * HALF, l0);
+          tmem_ld16(tt + 5 * HALF, l1);
+          tmem_wait_ld();
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            u1[k] = (l0[k] + l1[k]) * (sTi * st[j * P.nvpad + b0 + c0 + k]);
+          if (same) {
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              g2[k] = g1[k];
+              u2[k] = u1[k];
+            }
+          } else {
+            tmem_ld16(tt + 2 * HALF, l0);
+            tmem_ld16(tt + 3 * HALF, l1);
+            tmem_wait_ld();
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+              g2[k] = (l0[k] + l1[k]) * (sCj * sc[i * P.nvpad + b0 + c0 + k]);
+            tmem_ld16(tt + 6 * HALF, l0);
+            tmem_ld16(tt + 7 * HALF, l1);
+            tmem_wait_ld();
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+              u2[k] = (l0[k] + l1[k]) * (sTj * st[i * P.nvpad + b0 + c0 + k]);
+          }
+        }
+        float ef = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const float2 eb = P.ev2[b0 + c0 + k];
+          const float dh = dh0 - eb.x;
+          const float bz = dh - dh0;
+          const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
+          const float r = __frcp_rn(d);
+          float num = g1[k] * fmaf(2.0f, u1[k], -u2[k]);
+          if (!diag) num = fmaf(g2[k], fmaf(2.0f, u2[k], -u1[k]), num);
+          ef = fmaf(num, r, ef);
+        }
+        eacc += (double)ef;
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(accempty);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
+      if (lane == 0) redd[ew] = eacc;
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (ew == 0 && lane == 0) {
+        double tot = 0.0;
+#pragma unroll
+        for (int w = 0; w < NEPI; ++w) tot += redd[w];
+        P.part[qidx] = tot;
+      }
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      ++nloc;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+int eos_smem_bytes(int nsl, int nstage) {
+  return nstage * nsl * (PANEL_BYTES + HPANEL_BYTES) + 1024 + 512;
+}
+
 // Self-test of the bounded-wait path: one thread waits on an mbarrier that
 // nothing ever completes, with a short clock budget.  The wait must give up,
 // raise the CTA abort flag and record `code` in the device error word, and
@@ -1663,6 +2011,125 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
     split_gemm_kernel<2><<<(unsigned)nitems, 192, smem, s>>>(tA, tB, P);
   }
   count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+// Local-orbital fragment energy in the split form: slices of Calpha and of its
+// projected copy Ct in one buffer, one persistent split_eos_kernel launch,
+// compensated FP64 pair and total reductions.
+int split_eos_energy(const double *Ca, const double *Ct, int NBA, int nvirt, int nocc,
+                     const double *eo, const double *ev, double *Epair, double *Etot,
+                     int nslices, cudaStream_t s) {
+  const int nsl = nslices + 1;
+  auto encode = get_encode();
+  if (!encode) {
+    set_error("cuTensorMapEncodeTiled entry point unavailable");
+    return RIMP2_ERR_UNSUPPORTED;
+  }
+  FragDesc fh[2];
+  memset(fh, 0, sizeof fh);
+  const int nvpad = (nvirt + TILE - 1) / TILE * TILE;
+  const int nks = (NBA + KSTEP - 1) / KSTEP;
+  const int nt = nvpad / TILE;
+  const int ntp = nt * (nt + 1) / 2;
+  const long long ncol = (long long)nocc * nvpad;
+  const long long R = 2LL * nks * ncol;
+  const int npairs = nocc * (nocc + 1) / 2;
+  const long long nitems = (long long)npairs * ntp * 2;
+  if (R > 2147483647LL - TILE || nitems > 2147483647LL || ncol > 2147483647LL) {
+    set_error("split local-orbital energy: fragment too large (rows=%lld, items=%lld)", R, nitems);
+    return RIMP2_ERR_ARG;
+  }
+  for (int f = 0; f < 2; ++f) {
+    FragDesc &F = fh[f];
+    F.nocc = nocc;
+    F.nvirt = nvirt;
+    F.nvpad = nvpad;
+    F.NBA = NBA;
+    F.nks = nks;
+    F.ntp = ntp;
+    F.ncol = (int)ncol;
+    F.row_base = (long long)f * nks * ncol;
+    F.col_base = (long long)f * ncol;
+    F.Ca = f ? Ct : Ca;
+    F.eo = eo;
+    F.ev = ev;
+  }
+  DevBuf frags, slices, inv, eo2, ev2, part, queue, pairs;
+  RIMP2_TRY(frags.alloc(sizeof fh, s));
+  RIMP2_TRY(slices.alloc(sizeof(__half) * (size_t)nsl * R * 64, s));
+  RIMP2_TRY(inv.alloc(sizeof(float) * 2 * (size_t)ncol, s));
+  RIMP2_TRY(eo2.alloc(sizeof(float2) * nocc, s));
+  RIMP2_TRY(ev2.alloc(sizeof(float2) * nvpad, s));
+  RIMP2_TRY(part.alloc(sizeof(double) * (size_t)nitems, s));
+  RIMP2_TRY(queue.alloc(sizeof(unsigned int), s));
+  RIMP2_TRY(pairs.alloc(sizeof(int) * 2 * (size_t)npairs, s));
+  RIMP2_CK(cudaMemcpyAsync(frags.p, fh, sizeof fh, cudaMemcpyHostToDevice, s));
+  const FragDesc *fr = frags.as<FragDesc>();
+  slice_batch_kernel<<<dim3((unsigned)((ncol * 32 + 255) / 256), 2), 256, 0, s>>>(
+      fr, nsl, R * 64, slices.as<__half>(), inv.as<float>(), 0, 0x7fffffff);
+  eps_batch_kernel<<<dim3((unsigned)((std::max(nvpad, nocc) + 255) / 256), 1), 256, 0, s>>>(
+      fr, eo2.as<float2>(), ev2.as<float2>());
+  count_launch(2);
+  CUtensorMap tmA, tmB;
+  cuuint64_t dims[3] = {64, (cuuint64_t)R, (cuuint64_t)nsl};
+  cuuint64_t strides[2] = {128, (cuuint64_t)R * 128};
+  cuuint32_t boxA[3] = {KSTEP, TILE, 1}, boxB[3] = {KSTEP, HALF, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult cr = encode(&tmA, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, slices.p, dims, strides, boxA,
+                       estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr == CUDA_SUCCESS)
+    cr = encode(&tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, slices.p, dims, strides, boxB, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+    return RIMP2_ERR_CUDA;
+  }
+  EosParams P;
+  P.inv = inv.as<float>();
+  P.eo2 = eo2.as<float2>();
+  P.ev2 = ev2.as<float2>();
+  P.nitems = nitems;
+  P.queue = queue.as<unsigned int>();
+  P.part = part.as<double>();
+  P.err = device_error_word();
+  P.nocc = nocc;
+  P.nvirt = nvirt;
+  P.nvpad = nvpad;
+  P.nks = nks;
+  P.ntp = ntp;
+  P.ncol = (int)ncol;
+  P.rowC = 0;
+  P.rowCt = (int)((long long)nks * ncol);
+  int dev = 0, nsm = 0;
+  RIMP2_CK(cudaGetDevice(&dev));
+  RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = (int)std::min<long long>(nitems, nsm);
+  RIMP2_CK(cudaMemsetAsync(queue.p, 0, sizeof(unsigned int), s));
+  if (inject_fault("launch")) {
+    set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
+    return RIMP2_ERR_CUDA;
+  }
+  if (nsl == 2) {
+    RIMP2_CK(cudaFuncSetAttribute(split_eos_kernel<2, 4>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, eos_smem_bytes(2, 4)));
+    split_eos_kernel<2, 4><<<grid, NTHREADS, eos_smem_bytes(2, 4), s>>>(tmA, tmB, P);
+  } else {
+    RIMP2_CK(cudaFuncSetAttribute(split_eos_kernel<3, 3>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, eos_smem_bytes(3, 3)));
+    split_eos_kernel<3, 3><<<grid, NTHREADS, eos_smem_bytes(3, 3), s>>>(tmA, tmB, P);
+  }
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  make_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(nocc, pairs.as<int>());
+  RIMP2_CK(cudaMemsetAsync(Epair, 0, sizeof(double) * (size_t)nocc * nocc, s));
+  pair_reduce_kernel<<<(npairs + 7) / 8, 256, 0, s>>>(part.as<double>(), 2 * ntp, pairs.as<int>(),
+                                                     npairs, nocc, Epair);
+  total_reduce_kernel<<<1, 1024, 0, s>>>(Epair, nocc, Etot);
+  count_launch(3);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;
 }

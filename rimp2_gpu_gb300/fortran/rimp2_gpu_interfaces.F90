@@ -130,10 +130,10 @@ module rimp2_gpu_interfaces
 
      ! fused fragment energies (occupied and virtual partitioning) for general U
      integer(C_INT) function rimp2_energy_eos(nvirt, nocc, noccEOS, nvirtEOS, NBA, Calpha, EVocc, &
-          & EVvirt, UoccEOST, UvirtT, UoccT, UvirtEOST, Eocc, Evirt) &
+          & EVvirt, UoccEOST, UvirtT, UoccT, UvirtEOST, Eocc, Evirt, precision) &
           & bind(C, name="rimp2_energy_eos")
        import :: C_INT, C_DOUBLE
-       integer(C_INT), intent(in) :: nvirt, nocc, noccEOS, nvirtEOS, NBA
+       integer(C_INT), intent(in) :: nvirt, nocc, noccEOS, nvirtEOS, NBA, precision
        real(C_DOUBLE), intent(in) :: Calpha(NBA,nvirt,nocc), EVocc(nocc), EVvirt(nvirt)
        real(C_DOUBLE), intent(in) :: UoccEOST(nocc,noccEOS), UvirtT(nvirt,nvirt)
        real(C_DOUBLE), intent(in) :: UoccT(nocc,nocc), UvirtEOST(nvirt,nvirtEOS)

@@ -104,3 +104,34 @@ def test_split_large_K_exactness_bound(api, nslices):
     Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
     Ep, E = dev_energy(api, Ca, eo, ev, nslices)
     assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 1e-7
+
+
+@pytest.mark.parametrize("nocc,nvirt,NBA,noE,nvE", [(8, 96, 256, 3, 24), (16, 200, 512, 5, 40),
+                                                   (12, 256, 1024, 4, 64), (5, 130, 300, 5, 130)])
+def test_split_eos_energy_vs_fp64(nocc, nvirt, NBA, noE, nvE):
+    """Split-form local-orbital fragment energies within 1e-7 of the FP64
+    fused form (random orthonormal local blocks; the last case has
+    noccEOS = nocc and nvirtEOS = nvirt)."""
+    from oracle import oracle as O
+    from rimp2_gpu_gb300 import api
+    Ca, eo, ev = O.gen_fragment(40 + nocc, nocc, nvirt, NBA)
+
+    def q(m, k, s):
+        return np.asfortranarray(np.linalg.qr(O.gen_matrix(40 + nocc, s, m, m))[0][:, :k])
+    U = (q(nocc, noE, 1), q(nvirt, nvirt, 2), q(nocc, nocc, 3), q(nvirt, nvE, 4))
+    ref = api.energy_eos(nvirt, nocc, noE, nvE, NBA, Ca, eo, ev, *U, precision=api.PREC_FP64)
+    got = api.energy_eos(nvirt, nocc, noE, nvE, NBA, Ca, eo, ev, *U, precision=api.PREC_SPLIT)
+    for r, g in zip(ref, got):
+        assert abs(g - r) <= 1e-7 * abs(r), (g, r)
+
+
+def test_split_eos_identity_is_canonical():
+    from oracle import oracle as O
+    from rimp2_gpu_gb300 import api
+    nocc, nvirt, NBA = 9, 160, 640
+    Ca, eo, ev = O.gen_fragment(77, nocc, nvirt, NBA)
+    Io, Iv = np.eye(nocc, order="F"), np.eye(nvirt, order="F")
+    eocc, evir = api.energy_eos(nvirt, nocc, nocc, nvirt, NBA, Ca, eo, ev, Io, Iv, Io, Iv,
+                                precision=api.PREC_SPLIT)
+    _, E = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+    assert abs(eocc - E) <= 1e-7 * abs(E) and abs(evir - E) <= 1e-7 * abs(E)
