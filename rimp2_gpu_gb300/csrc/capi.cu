@@ -365,6 +365,61 @@ int dev_dgemm(char ta, char tb, int M, int N, int K, double alpha, const double 
 
 bool pos(const int *p) { return p && *p > 0; }
 
+// TransAlpha2 with the transformation matrix given by strides:
+// CD5(al,n3,n2) = sum_n1 U(n1,n3) CD4(al,n1,n2), U(k,n) = U[k*sUk + n*sUn]
+int dev_transalpha2_strided(int n2, int n1, int n3, int nba, const double *U, long long sUk,
+                            long long sUn, const double *CD4, double *CD5, cudaStream_t s) {
+  GemmDesc g = gd();
+  const long long b = nba;
+  g.M = nba;
+  g.N = n3;
+  g.K = n1;
+  g.A = CD4;
+  g.sAm = 1;
+  g.sAk = b;
+  g.sAb0 = b * n1;
+  g.B = U;
+  g.sBk = sUk;
+  g.sBn = sUn;
+  g.C = CD5;
+  g.sCm = 1;
+  g.sCn = b;
+  g.sCb0 = b * n3;
+  g.nb0 = n2;
+  return launch_gemm_f64(g, s);
+}
+
+// max |P(i,j) - delta_ij| over an n x n matrix (one block)
+__global__ void identity_dev_kernel(const double *P, int n, double *out) {
+  __shared__ double red[32];
+  double m = 0.0;
+  const long long nn = (long long)n * n;
+  for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
+    const long long i = t % n, j = t / n;
+    m = fmax(m, fabs(P[t] - (i == j ? 1.0 : 0.0)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+    *out = r;
+  }
+}
+
+// true if P = I within 1e-13 (P on the device; synchronises s)
+int is_identity(const double *P, int n, double *dwork, bool *yes, cudaStream_t s) {
+  identity_dev_kernel<<<1, 1024, 0, s>>>(P, n, dwork);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  double h = 1.0;
+  RIMP2_CK(cudaMemcpyAsync(&h, dwork, sizeof h, cudaMemcpyDeviceToHost, s));
+  RIMP2_CK(cudaStreamSynchronize(s));
+  *yes = (h <= 1e-13);
+  return RIMP2_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -772,7 +827,7 @@ int rimp2_energy_eos(const int *nvirt_, const int *nocc_, const int *noccEOS_,
   const int nvirt = *nvirt_, nocc = *nocc_, noccEOS = *noccEOS_, nvirtEOS = *nvirtEOS_,
             NBA = *NBA_;
   const size_t nv = nvirt, no = nocc, ne = noccEOS, ve = nvirtEOS, nb = NBA;
-  DevBuf dC, deo, dev, dUoE, dUvT, dUoT, dUvE, Po, Pv, C2, Ct, Ep, Et;
+  DevBuf dC, deo, dev, dUoE, dUvT, dUoT, dUvE, Po, Pv, C1, C2, D1, Ct, Ep, Et, wk;
   RIMP2_TRY(h2d(dC, Calpha, nb * nv * no, s));
   RIMP2_TRY(h2d(deo, EVocc, no, s));
   RIMP2_TRY(h2d(dev, EVvirt, nv, s));
@@ -780,34 +835,63 @@ int rimp2_energy_eos(const int *nvirt_, const int *nocc_, const int *noccEOS_,
   RIMP2_TRY(h2d(dUvT, UvirtT, nv * nv, s));
   RIMP2_TRY(h2d(dUoT, UoccT, no * no, s));
   RIMP2_TRY(h2d(dUvE, UvirtEOST, nv * ve, s));
+  const int kmax = std::max(noccEOS, nocc), vmax = std::max(nvirtEOS, nvirt);
   RIMP2_TRY(dalloc(Po, no * no, s));
   RIMP2_TRY(dalloc(Pv, nv * nv, s));
+  RIMP2_TRY(dalloc(C1, nb * nv * (size_t)kmax, s));
   RIMP2_TRY(dalloc(C2, nb * nv * no, s));
+  RIMP2_TRY(dalloc(D1, nb * (size_t)vmax * no, s));
   RIMP2_TRY(dalloc(Ct, nb * nv * no, s));
   RIMP2_TRY(dalloc(Ep, no * no, s));
   RIMP2_TRY(dalloc(Et, 2, s));
+  RIMP2_TRY(dalloc(wk, 1, s));
   const double *Uo[2] = {dUoE.as<double>(), dUoT.as<double>()};
   const double *Uv[2] = {dUvT.as<double>(), dUvE.as<double>()};
   const int ko[2] = {noccEOS, nocc}, kv[2] = {nvirt, nvirtEOS};
+  const long long MV = (long long)NBA * nvirt;
   for (int part = 0; part < 2; ++part) {
-    // projectors Po = Uo Uo^T, Pv = Uv Uv^T
-    RIMP2_TRY(dev_dgemm('N', 'T', nocc, nocc, ko[part], 1.0, Uo[part], nocc, Uo[part], nocc, 0.0,
-                        Po.as<double>(), nocc, s));
-    RIMP2_TRY(dev_dgemm('N', 'T', nvirt, nvirt, kv[part], 1.0, Uv[part], nvirt, Uv[part], nvirt,
-                        0.0, Pv.as<double>(), nvirt, s));
-    // Ct(:,a,i) = sum_c Pv(c,a) sum_k Calpha(:,c,k) Po(k,i)
-    RIMP2_TRY(dev_dgemm('N', 'N', NBA * nvirt, nocc, nocc, 1.0, dC.as<double>(), NBA * nvirt,
-                        Po.as<double>(), nocc, 0.0, C2.as<double>(), NBA * nvirt, s));
-    RIMP2_TRY(dev_transalpha2(nocc, nvirt, nvirt, NBA, Pv.as<double>(), C2.as<double>(),
-                              Ct.as<double>(), s));
+    // occupied side: C2(:,c,i) = sum_k Calpha(:,c,k) Po(k,i), Po = Uo Uo^T
+    const double *c2 = C2.as<double>();
+    if (2 * ko[part] <= nocc) {  // low rank: (Calpha Uo) Uo^T
+      RIMP2_TRY(dev_dgemm('N', 'N', (int)MV, ko[part], nocc, 1.0, dC.as<double>(), (int)MV,
+                          Uo[part], nocc, 0.0, C1.as<double>(), (int)MV, s));
+      RIMP2_TRY(dev_dgemm('N', 'T', (int)MV, nocc, ko[part], 1.0, C1.as<double>(), (int)MV,
+                          Uo[part], nocc, 0.0, C2.as<double>(), (int)MV, s));
+    } else {
+      RIMP2_TRY(dev_dgemm('N', 'T', nocc, nocc, ko[part], 1.0, Uo[part], nocc, Uo[part], nocc, 0.0,
+                          Po.as<double>(), nocc, s));
+      bool id = false;
+      RIMP2_TRY(is_identity(Po.as<double>(), nocc, wk.as<double>(), &id, s));
+      if (id)
+        c2 = dC.as<double>();  // orthogonal Uo: Po = I
+      else
+        RIMP2_TRY(dev_dgemm('N', 'N', (int)MV, nocc, nocc, 1.0, dC.as<double>(), (int)MV,
+                            Po.as<double>(), nocc, 0.0, C2.as<double>(), (int)MV, s));
+    }
+    // virtual side: Ct(:,a,i) = sum_c Pv(c,a) C2(:,c,i), Pv = Uv Uv^T
+    const double *ct = Ct.as<double>();
+    if (2 * kv[part] <= nvirt) {  // low rank: Uv (Uv^T C2)
+      RIMP2_TRY(dev_transalpha2(nocc, nvirt, kv[part], NBA, Uv[part], c2, D1.as<double>(), s));
+      RIMP2_TRY(dev_transalpha2_strided(nocc, kv[part], nvirt, NBA, Uv[part], nvirt, 1,
+                                        D1.as<double>(), Ct.as<double>(), s));
+    } else {
+      RIMP2_TRY(dev_dgemm('N', 'T', nvirt, nvirt, kv[part], 1.0, Uv[part], nvirt, Uv[part], nvirt,
+                          0.0, Pv.as<double>(), nvirt, s));
+      bool id = false;
+      RIMP2_TRY(is_identity(Pv.as<double>(), nvirt, wk.as<double>(), &id, s));
+      if (id)
+        ct = c2;  // orthogonal Uv: Pv = I
+      else
+        RIMP2_TRY(dev_transalpha2(nocc, nvirt, nvirt, NBA, Pv.as<double>(), c2, Ct.as<double>(),
+                                  s));
+    }
     if (*precision == RIMP2_PREC_SPLIT)
-      RIMP2_TRY(split_eos_energy(dC.as<double>(), Ct.as<double>(), NBA, nvirt, nocc,
-                                 deo.as<double>(), dev.as<double>(), Ep.as<double>(),
-                                 Et.as<double>() + part, rimp2_split_nslices(nvirt, nocc, NBA), s));
+      RIMP2_TRY(split_eos_energy(dC.as<double>(), ct, NBA, nvirt, nocc, deo.as<double>(),
+                                 dev.as<double>(), Ep.as<double>(), Et.as<double>() + part,
+                                 rimp2_split_nslices(nvirt, nocc, NBA), s));
     else
-      RIMP2_TRY(eos_energy_f64(dC.as<double>(), Ct.as<double>(), NBA, nvirt, nocc,
-                               deo.as<double>(), dev.as<double>(), Ep.as<double>(),
-                               Et.as<double>() + part, s));
+      RIMP2_TRY(eos_energy_f64(dC.as<double>(), ct, NBA, nvirt, nocc, deo.as<double>(),
+                               dev.as<double>(), Ep.as<double>(), Et.as<double>() + part, s));
   }
   double h[2];
   RIMP2_CK(cudaMemcpyAsync(h, Et.p, sizeof h, cudaMemcpyDeviceToHost, s));
