@@ -71,9 +71,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="CPU-baseline sample length; 0 skips it")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e leg")
-    ap.add_argument("--workload", choices=["fragment", "batched", "ao"], default="fragment",
+    ap.add_argument("--workload", choices=["fragment", "batched", "ao", "eos"],
+                    default="fragment",
                     help="fragment: one nocc=128/nvirt=1024/NBA=4096 fragment (default); "
-                         "batched: 256 uneven fragments in one graph-launched persistent kernel")
+                         "batched: 256 uneven fragments in one graph-launched persistent kernel; "
+                         "ao: 64 fragments from AO integrals; eos: local-orbital fragment "
+                         "energies at the reference's production shape")
     ap.add_argument("--batch-fragments", type=int, default=256,
                     help="batched workload: the first N of the 256 seeded shapes (profiling)")
     ap.add_argument("--ao-fragments", type=int, default=AO_N_DEFAULT,
@@ -801,10 +804,88 @@ def run_ao(args):
     return 0
 
 
+EOS_SHAPE = dict(nvirt=741, nocc=59, noccEOS=14, nvirtEOS=45, NBA=2173)  # generate.F90:48-53
+
+
+def run_eos(args):
+    """DEC fragment energies (occupied and virtual partitioning) with local
+    orbitals at the production shape that generate.F90 lists for its first
+    file, through the public host call rimp2_energy_eos: split form timed,
+    FP64 form once for the accuracy check and as the plain reference."""
+    import torch
+    from oracle import oracle as O
+    from rimp2_gpu_gb300 import api
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    nv, no, ne, ve, nb = (EOS_SHAPE[k] for k in ("nvirt", "nocc", "noccEOS", "nvirtEOS", "NBA"))
+    st = torch.cuda.Stream()
+    dC = torch.empty(nb * nv * no, dtype=torch.float64, device="cuda")
+    deo = torch.empty(no, dtype=torch.float64, device="cuda")
+    dev_ = torch.empty(nv, dtype=torch.float64, device="cuda")
+    api.gen_fragment_dev(6, no, nv, nb, dC.data_ptr(), deo.data_ptr(), dev_.data_ptr(),
+                         stream=st.cuda_stream)
+    st.synchronize()
+    Ca = np.asfortranarray(dC.cpu().numpy().reshape(nb, nv, no, order="F"))
+    eo, ev = deo.cpu().numpy(), dev_.cpu().numpy()
+
+    def orth(m, k, stream):  # orthonormal local-orbital blocks (QR of a seeded Gaussian)
+        return np.asfortranarray(np.linalg.qr(O.gen_matrix(6, stream, m, m))[0][:, :k])
+    U = (orth(no, ne, 1), orth(nv, nv, 2), orth(no, no, 3), orth(nv, ve, 4))
+    eff = 2 * 2 * 2.0 * nb * (no * nv) ** 2  # g and gt, both partitionings
+    for _ in range(args.warmup):
+        api.energy_eos(nv, no, ne, ve, nb, Ca, eo, ev, *U, precision=api.PREC_SPLIT)
+    barrier(pg)
+    torch.cuda.synchronize()
+    n0 = api.kernel_launch_count()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = api.energy_eos(nv, no, ne, ve, nb, Ca, eo, ev, *U, precision=api.PREC_SPLIT)
+        torch.cuda.synchronize()
+        sec = allmax(pg, (time.perf_counter() - t0) / args.steps)
+    launches = api.kernel_launch_count() - n0
+    acc = plain = None
+    if args.check == "full":
+        t0 = time.perf_counter()
+        ref = api.energy_eos(nv, no, ne, ve, nb, Ca, eo, ev, *U, precision=api.PREC_FP64)
+        psec = time.perf_counter() - t0
+        acc = {"Eocc_rel_err": abs(res[0] - ref[0]) / abs(ref[0]),
+               "Evirt_rel_err": abs(res[1] - ref[1]) / abs(ref[1]),
+               "within_1e-7": bool(abs(res[0] - ref[0]) <= 1e-7 * abs(ref[0]) and
+                                   abs(res[1] - ref[1]) <= 1e-7 * abs(ref[1])),
+               "against": "FP64 fused form"}
+        plain = {"s": psec, "eff_tflops": eff / psec / 1e12}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": world * eff / sec / 1e12, "unit": "TFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f16 Ozaki slices, f32 tensor accumulation (exact integer part), f64 "
+                     "projections and reductions",
+            "data": "synthetic (seeded Philox Calpha, QR-orthonormal local-orbital blocks)",
+            "config": {"workload": "DEC fragment energies, occupied and virtual partitioning, "
+                                   "through the host call rimp2_energy_eos (Calpha copy, "
+                                   "projections and both energies per step)", **EOS_SHAPE,
+                       "eff_flop_per_step": eff, "parallelism": f"replicas x{world}"},
+            "accuracy": acc, "plain_fp64": plain,
+            "e2e": {"value": world * eff / sec / 1e12, "unit": "TFLOP/s",
+                    "h2d_bytes_per_step": 8 * (nb * nv * no + no + nv + no * ne + nv * nv +
+                                               no * no + nv * ve),
+                    "d2h_bytes_per_step": 16},
+            "gpu_launches": launches, "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     if args.workload == "ao" and args.impl == "ours":
         return run_ao(args)
+    if args.workload == "eos" and args.impl == "ours":
+        return run_eos(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":

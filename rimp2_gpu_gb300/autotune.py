@@ -36,6 +36,9 @@ def _sample(lo, hi):
 
 
 SAMPLE = {lo: _sample(lo, hi) for lo, hi in zip(BUCKET_EDGES, BUCKET_TOP)}
+# the top bucket also covers the production fragment shapes the reference's
+# generator lists (generate.F90:48-53,65-70: nvirt 741/1041, nocc 59/99, NBA 2173)
+SAMPLE[BUCKET_EDGES[-1]] += [(59, 741, 2173), (99, 1041, 2173)]
 
 
 def _run(nocc, nvirt, NBA, seed):
