@@ -285,9 +285,9 @@ def run_reference(args):
 
 def run_e2e(args, api, torch, pg, world, Ca_np, eo_host, ev_host):
     """K steps of the public host-pointer call (copies inside the timed region).
-    The host-device link of this machine comes out of an idle period slowly
-    (after the minute-long FP64 check the first 4.3 GB copies run at a
-    fraction of the 211 GB/s steady rate), so the leg gets at least three
+    After an idle period (the minute-long FP64 check) the first calls run
+    several times slower while the SM clocks stay at their maximum (the
+    4.3 GB copy runs below its steady rate), so the leg gets at least three
     untimed warm-up calls."""
     for _ in range(max(3, args.warmup)):
         api.energy(NVIRT, NOCC, NBA, Ca_np, eo_host, ev_host, precision=api.PREC_SPLIT)
