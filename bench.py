@@ -613,7 +613,8 @@ def run_batched(args):
     if not args.no_e2e:
         host = [(t["C"].cpu().numpy().reshape(b, v, o, order="F"), t["eo"].cpu().numpy(),
                  t["ev"].cpu().numpy()) for t, (o, v, b) in zip(frags, shapes)]
-        api.energy_batched(host, precision=api.PREC_SPLIT)  # warm
+        for _ in range(max(3, args.warmup)):  # warm (see run_e2e)
+            api.energy_batched(host, precision=api.PREC_SPLIT)
         barrier(pg)
         t0 = time.perf_counter()
         for _ in range(args.steps):
