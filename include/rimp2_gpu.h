@@ -227,7 +227,8 @@ int rimp2_energy_fp64_noalloc_dev(int nvirt, int nocc, int NBA, const double *dC
                                   const double *dEVocc, const double *dEVvirt, double *dEpair,
                                   double *dEtot, void *stream);
 
-/* Split form with an explicit slice count (1 = S0+R1, 2 = S0+R1+R2). */
+/* Split form with an explicit slice count (1 = S0+R1, 2 = S0+R1+R2; 0 = the
+ * plain FP64 kernel, the table's tier for tiny fragments). */
 int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
                            const double *dEVocc, const double *dEVvirt, double *dEpair,
                            double *dEtot, int nslices, void *stream);
@@ -263,7 +264,10 @@ int rimp2_batch_plan_create(void **plan, int nfrag, const int *nocc, const int *
 int rimp2_batch_plan_execute(void *plan, void *stream);
 int rimp2_batch_plan_destroy(void *plan);
 /* Shape-bucket table of the split form: fragments with nvirt >= nvirt_min[k]
- * (largest such k) use nslices[k] residual slices (autotuner output). */
+ * (largest such k) use nslices[k] residual slices (autotuner output); 0 runs
+ * the fragment in FP64 (the default table does so below 16 virtuals, where a
+ * pair energy has too few (a,b) terms to average the split form's error).
+ * Every split-precision entry point follows the table. */
 int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices);
 
 /* ---- synthetic fragments (benchmark / test inputs; no counterpart in the

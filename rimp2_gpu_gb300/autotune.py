@@ -1,6 +1,7 @@
 """Shape-bucket autotuner for the split-precision energy path.
 
-For each virtual-space bucket it runs representative seeded fragments on the
+Below 16 virtuals fragments run in FP64 (slice count 0, a fixed rule).  For
+each larger virtual-space bucket it runs representative seeded fragments on the
 GPU three ways -- the plain FP64 kernel (the reference values) and the split
 kernel with one and with two residual slices -- and picks the cheapest slice
 count whose worst pair-energy relative error over the sample stays below
@@ -23,6 +24,7 @@ import numpy as np
 from . import api
 
 TARGET = 1e-7
+FP64_BELOW = 16  # fixed FP64 tier (slice count 0) below this many virtuals
 BUCKET_EDGES = [64, 128, 192, 256, 384]          # nvirt_min of each bucket
 BUCKET_TOP = [128, 192, 256, 384, 513]
 
@@ -87,10 +89,14 @@ def tune(seed=77):
                 worst[ns] = max(worst[ns], r[ns]["pair_max"], r[ns]["total"])
                 ms[ns] += r[ns]["ms"]
         pick = 1 if worst[1] <= TARGET / 2 else 2
-        table.append({"nvirt_min": lo if k else 0, "nslices": pick,
+        table.append({"nvirt_min": lo if k else FP64_BELOW, "nslices": pick,
                       "worst_rel_err": {"1": worst[1], "2": worst[2]},
                       "split_ms": {"1": ms[1], "2": ms[2]}, "sample": SAMPLE[lo]})
-    return {"target": TARGET, "margin": 0.5, "buckets": table}
+    fixed = {"nvirt_min": 0, "nslices": 0,
+             "rule": f"fragments with fewer than {FP64_BELOW} virtuals run in FP64: a pair "
+                     "energy of a few g^2 terms has nothing to average the split form's "
+                     "FP32-accumulated correction against"}
+    return {"target": TARGET, "margin": 0.5, "buckets": [fixed] + table}
 
 
 def apply(table):

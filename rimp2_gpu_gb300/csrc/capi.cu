@@ -885,10 +885,11 @@ int rimp2_energy_eos(const int *nvirt_, const int *nocc_, const int *noccEOS_,
         RIMP2_TRY(dev_transalpha2(nocc, nvirt, nvirt, NBA, Pv.as<double>(), c2, Ct.as<double>(),
                                   s));
     }
-    if (*precision == RIMP2_PREC_SPLIT)
+    const int ns = rimp2_split_nslices(nvirt, nocc, NBA);
+    if (*precision == RIMP2_PREC_SPLIT && ns > 0)
       RIMP2_TRY(split_eos_energy(dC.as<double>(), ct, NBA, nvirt, nocc, deo.as<double>(),
                                  dev.as<double>(), Ep.as<double>(), Et.as<double>() + part,
-                                 rimp2_split_nslices(nvirt, nocc, NBA), s));
+                                 ns, s));
     else
       RIMP2_TRY(eos_energy_f64(dC.as<double>(), ct, NBA, nvirt, nocc, deo.as<double>(),
                                dev.as<double>(), Ep.as<double>(), Et.as<double>() + part, s));
@@ -934,11 +935,16 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
 // Residual slices per element by shape bucket, chosen so that the pair and
 // total energies stay within 1e-7 relative of FP64: one residual slice
 // suffices once the pair sums average over enough (a,b) terms, small
-// fragments get two.  Buckets are keyed by nvirt (the (a,b) count per pair).
+// fragments get two, and fragments with fewer than 16 virtuals run in FP64
+// (0): their pair energies are a handful of g^2 terms, and a near-orthogonal
+// pair of columns (g ~ 1e-4 of the column norms) leaves the FP32-accumulated
+// correction term with nothing to average against (1.5e-5 measured at
+// nvirt = 1).  Buckets are keyed by nvirt (the (a,b) count per pair).
 // Default = the table measured by rimp2_gpu_gb300/autotune.py on GB300 with a
 // 2x margin on the 1e-7 target (rimp2_gpu_gb300/tuning/split_buckets.json);
 // rimp2_set_split_buckets replaces it.
-static std::vector<std::pair<int, int>> g_buckets = {{0, 2}, {128, 1}, {192, 1}, {256, 1}, {384, 1}};
+static std::vector<std::pair<int, int>> g_buckets = {{0, 0},   {16, 2},  {128, 1},
+                                                     {192, 1}, {256, 1}, {384, 1}};
 static std::mutex g_bucket_mu;
 
 int rimp2_split_nslices(int nvirt, int nocc, int NBA) {
@@ -956,7 +962,8 @@ int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices) {
   RIMP2_REQ(n > 0 && n <= 64 && nvirt_min && nslices, "rimp2_set_split_buckets: bad table");
   std::vector<std::pair<int, int>> t;
   for (int k = 0; k < n; ++k) {
-    RIMP2_REQ(nslices[k] == 1 || nslices[k] == 2, "rimp2_set_split_buckets: nslices must be 1 or 2");
+    RIMP2_REQ(nslices[k] >= 0 && nslices[k] <= 2,
+              "rimp2_set_split_buckets: nslices must be 0 (FP64), 1 or 2");
     RIMP2_REQ(k == 0 || nvirt_min[k] > nvirt_min[k - 1],
               "rimp2_set_split_buckets: nvirt_min must increase");
     t.push_back({nvirt_min[k], nslices[k]});
@@ -1015,9 +1022,25 @@ int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
   clear_error();
   RIMP2_REQ(nvirt > 0 && nocc > 0 && NBA > 0, "rimp2_energy_split_dev: bad dims");
   RIMP2_REQ(dCalpha && dEVocc && dEVvirt && dEpair && dEtot, "rimp2_energy_split_dev: null array");
-  RIMP2_REQ(nslices == 1 || nslices == 2, "rimp2_energy_split_dev: nslices must be 1 or 2");
+  RIMP2_REQ(nslices >= 0 && nslices <= 2,
+            "rimp2_energy_split_dev: nslices must be 0 (FP64), 1 or 2");
   RIMP2_TRY(ensure_device());
   cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
+  if (nslices == 0) {  // the bucket table's FP64 tier (tiny fragments)
+    PlainEnergyArgs p;
+    p.Ca = dCalpha;
+    p.NBA = NBA;
+    p.nvirt = nvirt;
+    p.nocc = nocc;
+    p.eo = dEVocc;
+    p.ev = dEVvirt;
+    p.Epair = dEpair;
+    p.Etot = dEtot;
+    p.tamp = nullptr;
+    p.pairs = nullptr;
+    p.npairs = 0;
+    return plain_energy_f64(p, s);
+  }
   SplitEnergyArgs a;
   a.Ca = dCalpha;
   a.NBA = NBA;
@@ -1045,7 +1068,8 @@ int rimp2_energy(const int *nvirt, const int *nocc, const int *NBA, const double
   cudaStream_t s = current_stream();
   const size_t nv = *nvirt, no = *nocc, nb = *NBA;
   DevBuf dC, deo, dev, dE, dT, dA;
-  if (*precision == RIMP2_PREC_SPLIT) {
+  // the bucket table sends tiny fragments to the FP64 kernel
+  if (*precision == RIMP2_PREC_SPLIT && rimp2_split_nslices(*nvirt, *nocc, *NBA) > 0) {
     // copy Calpha in occupied-index chunks overlapped with the energy work
     cudaStream_t cs = copy_stream();
     RIMP2_REQ(cs != nullptr, "rimp2_energy: copy stream unavailable");
