@@ -639,6 +639,25 @@ int plain_energy_f64_scratch(const PlainEnergyArgs &a, int *pairs_scratch, doubl
 }
 
 int plain_energy_f64(const PlainEnergyArgs &a, cudaStream_t s) {
+  if (!a.tamp && !a.pairs) {
+    // energies only, all pairs: the persistent form (one launch draining the
+    // queue of (pair, tile pair) items, as for a batch of one fragment)
+    PlainFrag F;
+    memset(&F, 0, sizeof F);
+    F.Ca = a.Ca;
+    F.eo = a.eo;
+    F.ev = a.ev;
+    F.Epair = a.Epair;
+    F.Etot = a.Etot;
+    F.nocc = a.nocc;
+    F.nvirt = a.nvirt;
+    F.NBA = a.NBA;
+    PlainPlan *P = nullptr;
+    RIMP2_TRY(plain_plan_create(&P, 1, &F, s));
+    const int rc = plain_plan_record(P, s);
+    plain_plan_destroy(P);  // workspace is released stream-ordered
+    return rc;
+  }
   const int ntile = (a.nvirt + TM - 1) / TM;
   const int ntp = ntile * (ntile + 1) / 2;
   const int npairs = a.pairs ? a.npairs : a.nocc * (a.nocc + 1) / 2;
@@ -717,6 +736,7 @@ int eos_energy_f64(const double *Ca, const double *Ct, int NBA, int nvirt, int n
 struct PlainPlan {
   int nfrag = 0, npairs_total = 0, grid = 0;
   long long nitems = 0;
+  std::vector<PlainFrag> fh;  // host copy of the descriptor table
   DevBuf frags, part, queue;
 };
 
@@ -754,14 +774,10 @@ int plain_plan_create(PlainPlan **out, int nfrag, const PlainFrag *in, cudaStrea
   int rc = P->frags.alloc(sizeof(PlainFrag) * (size_t)nfrag, s);
   if (rc == RIMP2_OK) rc = P->part.alloc(sizeof(double) * (size_t)std::max<long long>(item, 1), s);
   if (rc == RIMP2_OK) rc = P->queue.alloc(sizeof(unsigned int), s);
+  P->fh = fh;
   if (rc == RIMP2_OK &&
-      cudaMemcpyAsync(P->frags.p, fh.data(), sizeof(PlainFrag) * (size_t)nfrag,
+      cudaMemcpyAsync(P->frags.p, P->fh.data(), sizeof(PlainFrag) * (size_t)nfrag,
                       cudaMemcpyHostToDevice, s) != cudaSuccess) {
-    set_error("plain batch descriptor copy failed");
-    rc = RIMP2_ERR_CUDA;
-  }
-  // the descriptor copy reads fh: finish it before fh goes out of scope
-  if (rc == RIMP2_OK && cudaStreamSynchronize(s) != cudaSuccess) {
     set_error("plain batch descriptor copy failed");
     rc = RIMP2_ERR_CUDA;
   }
