@@ -42,9 +42,19 @@ __device__ __forceinline__ void dmma884(double &d0, double &d1, double a, double
 // ---------------------------------------------------------------------------
 // Generic strided batched GEMM
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async8(double *dst, const double *src, bool valid) {
+  // 8-byte global -> shared copy; an invalid element is zero-filled (no read)
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src),
+               "r"(valid ? 8 : 0)
+               : "memory");
+}
+
+// The 16-wide K slabs are double-buffered with cp.async: the next slab is in
+// flight while the DMMA loop consumes the current one.
 __global__ void __launch_bounds__(NTHR) gemm_f64_kernel(GemmDesc g) {
-  __shared__ double As[TM][KP];
-  __shared__ double Bs[TN][KP];
+  __shared__ double As[2][TM][KP];
+  __shared__ double Bs[2][TN][KP];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp & 1) * 32, wn = (warp >> 1) * 16;
   const int gid = lane >> 2, tig = lane & 3;
@@ -66,8 +76,8 @@ __global__ void __launch_bounds__(NTHR) gemm_f64_kernel(GemmDesc g) {
 #pragma unroll
         for (int y = 0; y < 2; ++y) acc[x][y][0] = acc[x][y][1] = 0.0;
 
-      for (int k0 = 0; k0 < g.K; k0 += TK) {
-        // stage A(m0:m0+64, k0:k0+16) and B(k0:k0+16, n0:n0+64)
+      // stage A(m0:m0+64, k0:k0+16) and B(k0:k0+16, n0:n0+64) into buffer buf
+      auto load_slab = [&](int buf, int k0) {
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
           int mm, kk;
@@ -79,7 +89,9 @@ __global__ void __launch_bounds__(NTHR) gemm_f64_kernel(GemmDesc g) {
             kk = (tid >> 6) + 4 * p;
           }
           const int m = m0 + mm, k = k0 + kk;
-          As[mm][kk] = (m < g.M && k < g.K) ? Ab[m * g.sAm + k * g.sAk] : 0.0;
+          const bool va = (m < g.M && k < g.K);
+          cp_async8(&As[buf][mm][kk], va ? Ab + (long long)m * g.sAm + (long long)k * g.sAk : Ab,
+                    va);
           int nn, kb;
           if (b_kcontig) {
             kb = tid & 15;
@@ -89,22 +101,36 @@ __global__ void __launch_bounds__(NTHR) gemm_f64_kernel(GemmDesc g) {
             kb = (tid >> 6) + 4 * p;
           }
           const int n = n0 + nn, kq = k0 + kb;
-          Bs[nn][kb] = (n < g.N && kq < g.K) ? Bb[kq * g.sBk + n * g.sBn] : 0.0;
+          const bool vb = (n < g.N && kq < g.K);
+          cp_async8(&Bs[buf][nn][kb], vb ? Bb + (long long)kq * g.sBk + (long long)n * g.sBn : Bb,
+                    vb);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      };
+
+      if (g.K > 0) load_slab(0, 0);
+      int cur = 0;
+      for (int k0 = 0; k0 < g.K; k0 += TK, cur ^= 1) {
+        if (k0 + TK < g.K) {
+          load_slab(cur ^ 1, k0 + TK);
+          asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+          asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
 #pragma unroll
         for (int ks = 0; ks < TK; ks += 4) {
           double af[4], bf[2];
 #pragma unroll
-          for (int x = 0; x < 4; ++x) af[x] = As[wm + 8 * x + gid][ks + tig];
+          for (int x = 0; x < 4; ++x) af[x] = As[cur][wm + 8 * x + gid][ks + tig];
 #pragma unroll
-          for (int y = 0; y < 2; ++y) bf[y] = Bs[wn + 8 * y + gid][ks + tig];
+          for (int y = 0; y < 2; ++y) bf[y] = Bs[cur][wn + 8 * y + gid][ks + tig];
 #pragma unroll
           for (int x = 0; x < 4; ++x)
 #pragma unroll
             for (int y = 0; y < 2; ++y) dmma884(acc[x][y][0], acc[x][y][1], af[x], bf[y]);
         }
-        __syncthreads();
+        __syncthreads();  // buffer cur is refilled two slabs later
       }
       // epilogue
 #pragma unroll
