@@ -779,9 +779,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   constexpr int NEPI = 8;
   uint8_t *stages = base;
   uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
-  // bars: full[NSTAGE], empty[NSTAGE], accfull, accempty, drain, item_full[IQ],
+  // bars: full[NSTAGE], empty[NSTAGE], tfull[4], tempty[4], drain, item_full[IQ],
   //       item_empty[IQ]
-  constexpr int NB = 2 * NSTAGE + 3 + 2 * IQ;
+  constexpr int NB = 2 * NSTAGE + 9 + 2 * IQ;
   uint32_t *tmem_slot = (uint32_t *)(bars + NB);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   volatile long long *item_q =
@@ -791,19 +791,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(&bars[0]);
   const uint32_t empty0 = smem_u32(&bars[NSTAGE]);
-  const uint32_t accfull = smem_u32(&bars[2 * NSTAGE]);
-  const uint32_t accempty = smem_u32(&bars[2 * NSTAGE + 1]);
-  const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 2]);
-  const uint32_t ifull0 = smem_u32(&bars[2 * NSTAGE + 3]);
-  const uint32_t iempty0 = smem_u32(&bars[2 * NSTAGE + 3 + IQ]);
+  const uint32_t tfull0 = smem_u32(&bars[2 * NSTAGE]);       // + 8 t
+  const uint32_t tempty0 = smem_u32(&bars[2 * NSTAGE + 4]);  // + 8 t
+  const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 8]);
+  const uint32_t ifull0 = smem_u32(&bars[2 * NSTAGE + 9]);
+  const uint32_t iempty0 = smem_u32(&bars[2 * NSTAGE + 9 + IQ]);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NSTAGE; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
     }
-    mbar_init(accfull, 1);
-    mbar_init(accempty, NEPI);
+    for (int t = 0; t < 4; ++t) {
+      mbar_init(tfull0 + 8 * t, 1);
+      mbar_init(tempty0 + 8 * t, NEPI);
+    }
     mbar_init(drain, 1);
     for (int s = 0; s < IQ; ++s) {
       mbar_init(ifull0 + 8 * s, 1);
@@ -824,6 +826,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // tiles in issue order o = 0..3: T1 (C), U1 (Ct), T2 (C), U2 (Ct), i.e. tile
+  // t = 2 (o & 1) + (o >> 1); i = j items skip T2/U2
 
   if (warp == 0) {
     // ------------------------------ TMA producer ------------------------------
@@ -847,7 +851,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         int i, j, tA, tB, h;
         eos_decode(P, qidx, i, j, tA, tB, h);
         const bool same = (i == j);
-        for (int t = 0; t < 4 && ok; ++t) {
+        for (int o = 0; o < 4 && ok; ++o) {
+          const int t = ((o & 1) << 1) | (o >> 1);
           if (same && (t & 1)) continue;  // T2 = T1, U2 = U1
           const int rowbase = (t < 2) ? P.rowC : P.rowCt;
           const int ia = (t & 1) ? j : i, ib = (t & 1) ? i : j;
@@ -892,7 +897,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int stage = 0, islot = 0;
       uint32_t phase = 0, iphase = 0;
       bool ok = true;
-      long long nloc = 0;
+      uint32_t used = 0, par = 0;  // per tile: committed before / commit count parity
       while (ok) {
         if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 6)) break;
         const long long qidx = item_q[islot];
@@ -905,15 +910,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         int i, j, tA, tB, h;
         eos_decode(P, qidx, i, j, tA, tB, h);
         const bool same = (i == j);
-        // the previous item's accumulators must have been read out
-        if (nloc > 0 &&
-            !mbar_wait(accempty, (uint32_t)((nloc - 1) & 1), abort_flag, P.err, 2)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        for (int t = 0; t < 4 && ok; ++t) {
+        for (int o = 0; o < 4 && ok; ++o) {
+          const int t = ((o & 1) << 1) | (o >> 1);
           if (same && (t & 1)) continue;
+          // the tile's previous accumulators must have been read out
+          if (((used >> t) & 1) &&
+              !mbar_wait(tempty0 + 8 * t, ((par >> t) & 1) ^ 1u, abort_flag, P.err, 2)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
           const uint32_t dL0 = tmem + (uint32_t)(t * 2 * HALF);
           const uint32_t dL1 = dL0 + HALF;
           for (int kc = 0; kc < P.nks; ++kc) {
@@ -949,10 +955,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               phase ^= 1;
             }
           }
+          if (!ok) break;
+          mma_commit(tfull0 + 8 * t);  // tile t of this item is complete
+          used |= 1u << t;
+          par ^= 1u << t;
         }
-        if (!ok) break;
-        mma_commit(accfull);
-        ++nloc;
       }
       // drain: all MMAs issued by this thread complete before TMEM is freed
       mma_commit(drain);
@@ -962,15 +969,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else {
     // ------------------------------ epilogue ----------------------------------
+    // T1 and U1 are read into registers and released first, so the next
+    // item's T1/U1 MMAs overlap this item's T2/U2 phase.
     const int ew = warp - 2;             // 0..7
     const int quad = warp & 3;
     const int cbase = (ew >> 2) * 32;    // 32 of the tile's 64 columns
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    const uint32_t tbase = tmem + lane_off + cbase;
     int islot = 0;
     uint32_t iphase = 0;
-    long long nloc = 0;
-    while (true) {
+    uint32_t par = 0;  // per tile: parity of the reads so far
+    bool ok = true;
+    while (ok) {
       if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7)) break;
       const long long qidx = item_q[islot];
       __syncwarp();
@@ -996,65 +1007,66 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float dh0 = sh - ea.x;
       const float bw = dh0 - sh;
       const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
-      if (!mbar_wait(accfull, (uint32_t)(nloc & 1), abort_flag, P.err, 4)) break;
-      tc_fence_after();
-      double eacc = 0.0;
-#pragma unroll 1
-      for (int c0 = 0; c0 < 32; c0 += 16) {
-        float g1[16], g2[16], u1[16], u2[16];
-        {
+      // one tile's 32 columns of this thread into registers, then release it
+      auto take = [&](int t, const float *sr, float srow, float (&v)[32]) -> bool {
+        if (!mbar_wait(tfull0 + 8 * t, (par >> t) & 1, abort_flag, P.err, 4)) return false;
+        tc_fence_after();
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 16) {
           float l0[16], l1[16];
-          const uint32_t tt = tmem + lane_off + cbase + c0;
-          tmem_ld16(tt + 0 * HALF, l0);
-          tmem_ld16(tt + 1 * HALF, l1);
+          tmem_ld16(tbase + t * 2 * HALF + c0, l0);
+          tmem_ld16(tbase + t * 2 * HALF + HALF + c0, l1);
           tmem_wait_ld();
 #pragma unroll
-          for (int k = 0; k < 16; ++k)
-            g1[k] = (l0[k] + l1[k]) * (sCi * sc[j * P.nvpad + b0 + c0 + k]);
-          tmem_ld16(tt + 4 * HALF, l0);
-          tmem_ld16(tt + 5 * HALF, l1);
-          tmem_wait_ld();
-#pragma unroll
-          for (int k = 0; k < 16; ++k)
-            u1[k] = (l0[k] + l1[k]) * (sTi * st[j * P.nvpad + b0 + c0 + k]);
-          if (same) {
-#pragma unroll
-            for (int k = 0; k < 16; ++k) {
-              g2[k] = g1[k];
-              u2[k] = u1[k];
-            }
-          } else {
-            tmem_ld16(tt + 2 * HALF, l0);
-            tmem_ld16(tt + 3 * HALF, l1);
-            tmem_wait_ld();
-#pragma unroll
-            for (int k = 0; k < 16; ++k)
-              g2[k] = (l0[k] + l1[k]) * (sCj * sc[i * P.nvpad + b0 + c0 + k]);
-            tmem_ld16(tt + 6 * HALF, l0);
-            tmem_ld16(tt + 7 * HALF, l1);
-            tmem_wait_ld();
-#pragma unroll
-            for (int k = 0; k < 16; ++k)
-              u2[k] = (l0[k] + l1[k]) * (sTj * st[i * P.nvpad + b0 + c0 + k]);
-          }
+          for (int k = 0; k < 16; ++k) v[c0 + k] = (l0[k] + l1[k]) * (srow * sr[b0 + c0 + k]);
         }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tempty0 + 8 * t);
+        par ^= 1u << t;
+        return true;
+      };
+      float g1[32], u1[32];
+      if (!take(0, sc + j * P.nvpad, sCi, g1) || !take(2, st + j * P.nvpad, sTi, u1)) {
+        ok = false;
+        break;
+      }
+      double eacc = 0.0;
+      if (same) {
         float ef = 0.0f;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const float2 eb = P.ev2[b0 + c0 + k];
+        for (int k = 0; k < 32; ++k) {
+          const float2 eb = P.ev2[b0 + k];
           const float dh = dh0 - eb.x;
           const float bz = dh - dh0;
           const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
-          const float r = __frcp_rn(d);
-          float num = g1[k] * fmaf(2.0f, u1[k], -u2[k]);
-          if (!diag) num = fmaf(g2[k], fmaf(2.0f, u2[k], -u1[k]), num);
-          ef = fmaf(num, r, ef);
+          // g2 = g1, u2 = u1: diagonal g1 u1, otherwise 2 g1 u1
+          ef = fmaf((diag ? 1.0f : 2.0f) * g1[k] * u1[k], __frcp_rn(d), ef);
         }
-        eacc += (double)ef;
+        eacc = (double)ef;
+      } else {
+        float g2[32], u2[32];
+        if (!take(1, sc + i * P.nvpad, sCj, g2) || !take(3, st + i * P.nvpad, sTj, u2)) {
+          ok = false;
+          break;
+        }
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 16) {
+          float ef = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const float2 eb = P.ev2[b0 + c0 + k];
+            const float dh = dh0 - eb.x;
+            const float bz = dh - dh0;
+            const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
+            const int c = c0 + k;
+            float num = g1[c] * fmaf(2.0f, u1[c], -u2[c]);
+            if (!diag) num = fmaf(g2[c], fmaf(2.0f, u2[c], -u1[c]), num);
+            ef = fmaf(num, __frcp_rn(d), ef);
+          }
+          eacc += (double)ef;
+        }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(accempty);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
       if (lane == 0) redd[ew] = eacc;
@@ -1066,7 +1078,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         P.part[qidx] = tot;
       }
       asm volatile("bar.sync 1, 256;" ::: "memory");
-      ++nloc;
     }
   }
   tc_fence_before();
