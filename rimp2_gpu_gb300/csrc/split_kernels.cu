@@ -293,12 +293,19 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
   const double *c = F.Ca + ((size_t)i * F.nvirt + a) * NBA;
   unsigned long long mxb = 0;
   float ss = 0.0f;
-  for (int k = lane; k < NBA; k += 32) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(c[k]);
-    const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-    mxb = mag > mxb ? mag : mxb;
-    const float f = bits_to_float_trunc(mag, 0);
-    ss = fmaf(f, f, ss);
+  // four independent loads in flight per lane (the pass is latency-bound)
+  for (int k0 = lane; k0 < NBA; k0 += 128) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = (k0 + 32 * u < NBA) ? c[k0 + 32 * u] : 0.0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned long long mag =
+          (unsigned long long)__double_as_longlong(v[u]) & 0x7FFFFFFFFFFFFFFFull;
+      mxb = mag > mxb ? mag : mxb;
+      const float f = bits_to_float_trunc(mag, 0);
+      ss = fmaf(f, f, ss);
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -318,23 +325,31 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
   }
   for (int attempt = 0; attempt < 64; ++attempt) {
     long long n2 = 0;  // sum of S0^2 (integers; <= 2^24 is the test)
-    for (int k = lane; k < Kpad; k += 32) {
-      __half h0 = hz, h1 = hz, h2 = hz;
-      if (k < NBA) {
-        float xh, xl;
-        split_double(c[k], e, xh, xl);
-        const float q = rintf(xh);
-        const float r = (xh - q) + xl;  // xh - q exact
-        h0 = __float2half_rn(q);        // integer |q| <= 2048: exact in FP16
-        h1 = __float2half_rn(r);
-        h2 = __float2half_rn(r - __half2float(h1));
-        const int qi = (int)q;
-        n2 += (long long)qi * qi;
+    for (int k0 = lane; k0 < Kpad; k0 += 128) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = (k0 + 32 * u < NBA) ? c[k0 + 32 * u] : 0.0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 32 * u;
+        if (k >= Kpad) break;
+        __half h0 = hz, h1 = hz, h2 = hz;
+        if (k < NBA) {
+          float xh, xl;
+          split_double(v[u], e, xh, xl);
+          const float q = rintf(xh);
+          const float r = (xh - q) + xl;  // xh - q exact
+          h0 = __float2half_rn(q);        // integer |q| <= 2048: exact in FP16
+          h1 = __float2half_rn(r);
+          h2 = __float2half_rn(r - __half2float(h1));
+          const int qi = (int)q;
+          n2 += (long long)qi * qi;
+        }
+        const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
+        out[o] = h0;
+        if (nsl > 1) out[plane + o] = h1;
+        if (nsl > 2) out[2 * plane + o] = h2;
       }
-      const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
-      out[o] = h0;
-      if (nsl > 1) out[plane + o] = h1;
-      if (nsl > 2) out[2 * plane + o] = h2;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
