@@ -1680,6 +1680,13 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
                       double *const *Epair, double *const *Etot, const int *nslices, bool graph,
                       cudaStream_t s) {
   *out = nullptr;
+  // work items pack i | j << 16 and tA | tB << 16
+  for (int f = 0; f < nfrag; ++f)
+    if (nocc[f] > 65535 || (nvirt[f] + TILE - 1) / TILE > 65535) {
+      set_error("split form: fragment %d too large for the work-item encoding (nocc=%d)", f,
+                nocc[f]);
+      return RIMP2_ERR_ARG;
+    }
   SplitPlan *P = new SplitPlan();
   int dev = 0;
   cudaGetDevice(&dev);
