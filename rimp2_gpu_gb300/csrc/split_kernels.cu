@@ -17,15 +17,20 @@
 //   FP64 across threads; pair and total energies are reduced in FP64 with
 //   compensation.
 //
-// Kernel layout (one persistent CTA per SM, 192 threads):
-//   warp 0      TMA producer: 128x64 FP16 tiles (128B swizzle) of the slices
+// Kernel layout (one persistent CTA per SM, 320 threads):
+//   warp 0      TMA producer (128x64 FP16 boxes, 128B swizzle) and the
+//               device-side work queue (atomic counter, 4-deep item ring)
 //   warp 1      TMEM owner + single-thread tcgen05.mma issuer
-//   warps 2..5  epilogue: tcgen05.ld of the four accumulators, energy terms
-//   Work item = (pair i<=j, tile pair A<=B): T1 = G_ij[A,B] = C_iA^T C_jB and
-//   T2 = G_ji[A,B] = C_jA^T C_iB, each with L0/L1 accumulators in TMEM
-//   (4 x 128 columns = all 512).  The exchange integral g_ij(b,a) = T2[a,b]
-//   therefore lives in the same TMEM lane/column as g_ij(a,b) = T1[a,b], and
-//   no four-index quantity is ever written to memory.
+//   warps 2..9  epilogue, two warps per TMEM lane quadrant: tcgen05.ld of the
+//               accumulators, denominators, energy terms
+//   Work item = (fragment, pair i<=j, tile pair A<=B): T1 = G_ij[A,B] =
+//   C_iA^T C_jB and T2 = G_ji[A,B] = C_jA^T C_iB, each with L0/L1
+//   accumulators in TMEM (4 x 128 columns = all 512).  The exchange integral
+//   g_ij(b,a) = T2[a,b] therefore lives in the same TMEM lane/column as
+//   g_ij(a,b) = T1[a,b], and no four-index quantity is ever written to
+//   memory.  T1 is read out and released first, so the next item's T1 MMAs
+//   overlap this item's T2 phase; diagonal tile pairs take T2 = T1^T through
+//   shared memory.
 // Every wait on an mbarrier is bounded by a clock budget; on expiry the
 // kernel records an error code, drains its own copies and MMAs, frees TMEM
 // and returns, and the host reports RIMP2_ERR_TIMEOUT.
