@@ -5,16 +5,21 @@
 //    orbital-energy denominator epilogue.  It carries every FP64 product of
 //    the drop-in subroutines (toccA/tvirtA g/D and projections, toccB/tvirtB,
 //    TransAlpha1/2, gocc/gvirt/gen4DimFO, the driver's DGEMMs).
-//  * plain_energy_kernel: the fused FP64 energy kernel.  One CTA owns the tile
-//    pair (A,B) of occupied pair (i<=j): T1 = G_ij[A,B] = C_iA^T C_jB and
-//    T2 = G_ji[A,B] = C_jA^T C_iB share the (a,b) layout, so the exchange
-//    integral g_ij(b,a) sits in the same thread as g_ij(a,b) and the
-//    four-index integrals never leave the chip.
+//  * the fused FP64 energy: a work item is the tile pair (A,B) of occupied
+//    pair (i<=j): T1 = G_ij[A,B] = C_iA^T C_jB and T2 = G_ji[A,B] =
+//    C_jA^T C_iB share the (a,b) layout, so the exchange integral g_ij(b,a)
+//    sits in the same thread as g_ij(a,b) and the four-index integrals never
+//    leave the chip.  plain_batch_kernel is the persistent form (a queue of
+//    items over one or many fragments, the energy path); plain_energy_kernel
+//    runs one item per CTA and can also write the amplitude array.
+//  * eos_energy_kernel: the same items with a second, projected Calpha (the
+//    local-orbital fragment energy).
 //
 // GB300 FP64 throughput is a small fraction of its low-precision tensor
 // rate, so these kernels are arithmetic-bound by construction: shared-memory
-// staging is simple, padding keeps fragment loads bank-conflict free, and
-// the CTA count is large enough to fill all 152 SMs several times.
+// staging is simple (cp.async double buffering in the GEMM), padding keeps
+// fragment loads bank-conflict free, and two CTAs per SM keep the FP64 pipe
+// busy.
 #include "common.cuh"
 
 #include <algorithm>
