@@ -1,13 +1,14 @@
-// front_end.cu -- Calpha from AO three-centre integrals, all FP64 on the GPU.
+// front_end.cu -- Calpha from AO three-centre integrals on the GPU.
 //
 //   (alpha|a i) = sum_{mu,nu} Cmo(mu,nocc+a) Cmo(nu,i) (alpha|mu nu)
 //   V = L L^T (Cholesky of the auxiliary metric)
 //   Calpha(:,a,i) = L^{-1} (:|a i)
 // so that sum_alpha Calpha(alpha,a,i) Calpha(alpha,b,j) = (ai|V^{-1}|bj).
 // The reference starts from Calpha (RIMP2.F90:48-49); this front end has no
-// counterpart there.  Every product runs on the FP64 DMMA GEMM of
-// fp64_kernels.cu; the Cholesky and the solve are blocked (64) so that all
-// but O(n*64^2) of their work is GEMM:
+// counterpart there.  The AO->MO transform runs either on the FP64 DMMA GEMM
+// of fp64_kernels.cu or on the tcgen05 split GEMM (two residual FP16 slices,
+// ~2^-33 relative per product); the Cholesky and the solve are FP64, blocked
+// (64) so that all but O(n*64^2) of their work is GEMM:
 //   Cholesky: diagonal-block factorisation and inverse (one CTA), panel
 //             P L_kk^{-T} (GEMM), trailing update C -= P P^T on the
 //             lower-triangle tiles;
