@@ -183,6 +183,18 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// Reciprocal of an energy denominator (never zero or subnormal here): the
+// hardware approximation (PTX rcp.approx.ftz.f32, about one ulp) refined by
+// one Newton-Raphson step r' = r + r (1 - d r), whose residual 1 - d r is
+// exact in one FMA; the result is within about half an ulp, so a fragment
+// whose denominators are all equal does not accumulate a one-sided error.
+__device__ __forceinline__ float rcp_denom(float d) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+  const float e = fmaf(-d, r, 1.0f);
+  return fmaf(r, e, r);
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -680,7 +692,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const float dh = dh0 - eb.x;
           const float bz = dh - dh0;
           const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
-          const float r = __frcp_rn(d);
+          const float r = rcp_denom(d);
           const float num = diag ? x1 * fmaf(2.0f, x1, -x2) : 2.0f * fmaf(x1, x1 - x2, x2 * x2);
           ef = fmaf(num, r, ef);
         }
@@ -1061,7 +1073,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const float bz = dh - dh0;
           const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
           // g2 = g1, u2 = u1: diagonal g1 u1, otherwise 2 g1 u1
-          ef = fmaf((diag ? 1.0f : 2.0f) * g1[k] * u1[k], __frcp_rn(d), ef);
+          ef = fmaf((diag ? 1.0f : 2.0f) * g1[k] * u1[k], rcp_denom(d), ef);
         }
         eacc = (double)ef;
       } else {
@@ -1082,7 +1094,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const int c = c0 + k;
             float num = g1[c] * fmaf(2.0f, u1[c], -u2[c]);
             if (!diag) num = fmaf(g2[c], fmaf(2.0f, u2[c], -u1[c]), num);
-            ef = fmaf(num, __frcp_rn(d), ef);
+            ef = fmaf(num, rcp_denom(d), ef);
           }
           eacc += (double)ef;
         }
