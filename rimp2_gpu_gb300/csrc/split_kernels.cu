@@ -1848,8 +1848,12 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   const FragDesc *fr = g.frags.as<FragDesc>();
   int rc = RIMP2_OK;
   const int nchunk = (a.nocc + chunk_occ - 1) / chunk_occ;
-  std::vector<cudaEvent_t> ev(nchunk);
-  for (auto &e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  std::vector<cudaEvent_t> ev(nchunk, nullptr);
+  for (auto &e : ev)
+    if (rc == RIMP2_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      set_error("event creation failed");
+      rc = RIMP2_ERR_CUDA;
+    }
   const size_t slab = (size_t)a.NBA * a.nvirt;  // doubles per occupied index
   // copies first, so the copy engine runs ahead of the compute stream
   for (int c = 0; c < nchunk && rc == RIMP2_OK; ++c) {
@@ -1926,7 +1930,8 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
     cudaStreamSynchronize(copy_s);
     cudaStreamSynchronize(s);
   }
-  for (auto &e : ev) cudaEventDestroy(e);
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
   split_plan_destroy(P);
   return rc;
 }
