@@ -15,7 +15,9 @@
  *     process; rimp2_last_error_string() describes the last failure.  (The
  *     reference discards every cuBLAS status, RIMP2.GPU.F90:81,119,135.)
  * There is no CPU fallback: on a machine without a usable sm_103 GPU each
- * compute entry returns RIMP2_ERR_NODEV.
+ * compute entry returns RIMP2_ERR_NODEV.  The library works on the device
+ * that is current at its first compute call (its stream, error word and
+ * memory pool settings belong to that device); one process drives one GPU.
  */
 #ifndef RIMP2_GPU_H
 #define RIMP2_GPU_H
