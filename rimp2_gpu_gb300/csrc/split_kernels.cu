@@ -39,6 +39,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -257,6 +258,7 @@ struct FragDesc {
   long long row_base;   // first 64-wide slice row (per slice plane)
   long long col_base;   // first inverse-scale index
   long long item_base;  // first work item
+  long long pitem_base; // first pair item (paired-CTA kernel)
   const double *Ca, *eo, *ev;
   double *Epair, *Etot;
 };
@@ -766,6 +768,563 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }
 
 // ==========================================================================
+// Paired-CTA form of the energy kernel (cta_group::2 on a cluster of two
+// CTAs, M = 256).  The two CTAs of a pair evaluate the occupied pairs
+// (i0, j) and (i0 + 1, j) for the same tile pair (A, B):
+//   T1  = G_ij[A,B] = C_iA^T C_jB   (a on the TMEM lanes, b on the columns)
+//   T2' = G_ij[B,A] = C_iB^T C_jA   (b on the lanes, a on the columns)
+// Both products of an item have the same B operand in the two CTAs (C_jB,
+// then C_jA), so each SM stages only half of it (64 rows) and its tensor core
+// reads 6 KB of shared memory per 256x128x16 step instead of the 8 KB of a
+// 128x128x16 step in split_batch_kernel; with the one-CTA tile the operand
+// reads, not the arithmetic, set the pace.  T2' is transposed through shared
+// memory in the epilogue, so that g_ij(a,b) and g_ij(b,a) meet in one thread.
+// A pair item with i0 + 1 > j runs its second CTA as a dummy (results
+// discarded); i0 == j (then the second CTA is a dummy) and A == B need only
+// T1.  The even CTA of the pair (rank 0) owns the work queue, the TMA full
+// barriers (both CTAs' copies complete on them), the MMA issue and the
+// accumulator-empty barriers; its commits are multicast to both CTAs.  Every
+// wait is bounded; a timeout in either CTA aborts both.
+// --------------------------------------------------------------------------
+constexpr int BHALF = TILE / 2;                  // B rows staged per CTA
+constexpr int BPANEL_BYTES = BHALF * KSTEP * 2;  // 8 KB
+constexpr int PAIR_NSTAGE = 4;
+// kind::f16, A = B = F16, D = F32, K-major, M = 256 (pair), N = 128
+constexpr uint32_t IDESC_PAIR = (1u << 4) | ((uint32_t)(TILE >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// shared::cluster address of the same shared variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_shared(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;" ::
+          : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test_cl(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ void st_remote_u32(uint32_t cluster_addr, uint32_t v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cluster_addr), "r"(v) : "memory");
+}
+
+// TMA load into this CTA's shared memory whose completion is counted on the
+// pair's (rank 0) barrier
+__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap *map,
+                                                 uint32_t bar_cluster, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(bar_cluster), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_f16_pair(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC_PAIR), "r"(acc)
+      : "memory");
+}
+
+// arrive on the barrier at this shared offset in both CTAs of the pair once
+// all previously issued MMAs of this thread have completed
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(bar),
+      "h"((uint16_t)3)
+      : "memory");
+}
+
+// OR of a predicate over the 256 epilogue threads (named barrier 1)
+__device__ __forceinline__ bool epi_any(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, o;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred o, 1, 256, q;\n\t"
+      "selp.u32 %0, 1, 0, o;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p)
+      : "memory");
+  return r != 0;
+}
+
+// Bounded wait that also aborts the peer CTA on a timeout.
+__device__ __forceinline__ bool pair_wait(uint32_t bar, uint32_t parity, bool cluster_scope,
+                                          volatile int *abort_flag, uint32_t abort_peer, int *err,
+                                          int code) {
+  const long long t0 = clock64();
+  while (!(cluster_scope ? mbar_test_cl(bar, parity) : mbar_test(bar, parity))) {
+    if (*abort_flag) return false;
+    if (clock64() - t0 > WAIT_BUDGET) {
+      *abort_flag = 1;
+      st_remote_u32(abort_peer, 1u);
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+struct PairParams {
+  const FragDesc *frags;
+  const int4 *items;     // {fragment, i0 | j << 16, tA | tB << 16, tile pair index}
+  long long nitems;
+  unsigned int *queue;   // next item counter (reset per launch)
+  const float2 *eo2, *ev2;
+  const float *inv_scale;
+  double *part;          // indexed like split_batch_kernel's work items
+  int *err;
+};
+
+int pair_smem_bytes() {
+  return PAIR_NSTAGE * 2 * (PANEL_BYTES + BPANEL_BYTES) + 1024 + 512 + 64 * TP * 4;
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
+    split_pair_kernel(const __grid_constant__ CUtensorMap tmA,
+                      const __grid_constant__ CUtensorMap tmB, PairParams P) {
+  constexpr int NSL = 2;
+  constexpr int NSTAGE = PAIR_NSTAGE;
+  constexpr int STAGE_BYTES = NSL * (PANEL_BYTES + BPANEL_BYTES);  // 48 KB per CTA
+  constexpr int NEPI = 8;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *stages = base;
+  uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
+  // bars: full[NSTAGE], empty[NSTAGE], t1full, t1empty, t2full, t2empty, drain,
+  //       item_full[IQ], item_empty[IQ]
+  constexpr int NB = 2 * NSTAGE + 5 + 2 * IQ;
+  uint32_t *tmem_slot = (uint32_t *)(bars + NB);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  volatile int *item_q = (volatile int *)(tmem_slot + 2);  // [IQ]
+  double *redd = (double *)(((uintptr_t)(tmem_slot + 2 + IQ) + 7) & ~(uintptr_t)7);  // [NEPI]
+  float *tbuf = (float *)(base + NSTAGE * STAGE_BYTES + 512);  // [64][TP]
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();
+  const bool leader = rank == 0;
+  const uint32_t full0 = smem_u32(&bars[0]);
+  const uint32_t empty0 = smem_u32(&bars[NSTAGE]);
+  const uint32_t t1full = smem_u32(&bars[2 * NSTAGE]);
+  const uint32_t t1empty = smem_u32(&bars[2 * NSTAGE + 1]);
+  const uint32_t t2full = smem_u32(&bars[2 * NSTAGE + 2]);
+  const uint32_t t2empty = smem_u32(&bars[2 * NSTAGE + 3]);
+  const uint32_t drain = smem_u32(&bars[2 * NSTAGE + 4]);
+  const uint32_t ifull0 = smem_u32(&bars[2 * NSTAGE + 5]);
+  const uint32_t iempty0 = smem_u32(&bars[2 * NSTAGE + 5 + IQ]);
+  // the pair's shared barriers live in rank 0
+  const uint32_t full0_L = map_shared(full0, 0);
+  const uint32_t t1empty_L = map_shared(t1empty, 0);
+  const uint32_t t2empty_L = map_shared(t2empty, 0);
+  const uint32_t iempty0_L = map_shared(iempty0, 0);
+  const uint32_t abort_peer = map_shared(smem_u32((const void *)abort_flag), rank ^ 1u);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(full0 + 8 * s, 1);   // rank 0: its producer's arrive + both CTAs' bytes
+      mbar_init(empty0 + 8 * s, 1);  // multicast MMA commit
+    }
+    mbar_init(t1full, 1);
+    mbar_init(t1empty, 2 * NEPI);  // epilogue warps of both CTAs
+    mbar_init(t2full, 1);
+    mbar_init(t2empty, 2 * NEPI);
+    mbar_init(drain, 1);
+    for (int s = 0; s < IQ; ++s) {
+      mbar_init(ifull0 + 8 * s, 1);
+      mbar_init(iempty0 + 8 * s, 2 + 2 * NEPI);  // MMA issuer, peer producer, all epilogue warps
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync_all();  // both CTAs' barriers are initialised before any remote access
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // --------------------- TMA producers (both CTAs) ---------------------
+    if (lane == 0) {
+      const uint32_t item_q_peer = map_shared(smem_u32((const void *)item_q), 1);
+      const uint32_t ifull0_peer = map_shared(ifull0, 1);
+      int stage = 0, islot = 0;
+      uint32_t phase = 0, iphase = 0;
+      uint32_t armed = 0, armed_par = 0;  // rank 0: stages with copies expected, and parity
+      bool ok = true;
+      while (ok) {
+        int qidx;
+        if (leader) {
+          if (!pair_wait(iempty0 + 8 * islot, iphase ^ 1, true, abort_flag, abort_peer, P.err, 5))
+            break;
+          const long long id = (long long)atomicAdd(P.queue, 1u);
+          qidx = id < P.nitems ? (int)id : -1;
+          item_q[islot] = qidx;
+          st_remote_u32(item_q_peer + 4 * islot, (uint32_t)qidx);
+          mbar_arrive(ifull0 + 8 * islot);
+          mbar_arrive_remote(ifull0_peer + 8 * islot);
+        } else {
+          if (!pair_wait(ifull0 + 8 * islot, iphase, true, abort_flag, abort_peer, P.err, 5))
+            break;
+          qidx = item_q[islot];
+          mbar_arrive_remote(iempty0_L + 8 * islot);
+        }
+        if (++islot == IQ) {
+          islot = 0;
+          iphase ^= 1;
+        }
+        if (qidx < 0) break;
+        const int4 it = P.items[qidx];
+        const FragDesc &F = P.frags[it.x];
+        const int i0 = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
+        const int i = (i0 + (int)rank <= j) ? i0 + (int)rank : i0;  // a dummy loads i0's panels
+        const int ntiles = (tA == tB || i0 == j) ? 1 : 2;
+        for (int t = 0; t < ntiles && ok; ++t) {
+          const int colA = i * F.nvpad + (t == 0 ? tA : tB) * TILE;
+          const int colB = j * F.nvpad + (t == 0 ? tB : tA) * TILE + BHALF * (int)rank;
+          for (int kc = 0; kc < F.nks; ++kc) {
+            if (!pair_wait(empty0 + 8 * stage, phase ^ 1, false, abort_flag, abort_peer, P.err, 1)) {
+              ok = false;
+              break;
+            }
+            if (leader) {
+              mbar_expect_tx(full0 + 8 * stage, 2 * STAGE_BYTES);
+              armed |= 1u << stage;
+              armed_par = (armed_par & ~(1u << stage)) | (phase << stage);
+            }
+            const uint32_t dst = smem_u32(stages + stage * STAGE_BYTES);
+            const uint32_t fb = full0_L + 8 * stage;
+            const int rowk = (int)(F.row_base + (long long)kc * F.ncol);
+#pragma unroll
+            for (int sl = 0; sl < NSL; ++sl) {
+              tma_load_3d_pair(dst + sl * PANEL_BYTES, &tmA, fb, 0, rowk + colA, sl);
+              tma_load_3d_pair(dst + NSL * PANEL_BYTES + sl * BPANEL_BYTES, &tmB, fb, 0,
+                               rowk + colB, sl);
+            }
+            if (++stage == NSTAGE) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+      }
+      if (leader && (!ok || *abort_flag)) {  // copies in flight complete before the pair exits
+        for (int s = 0; s < NSTAGE; ++s) {
+          if (!((armed >> s) & 1u)) continue;
+          const long long t0 = clock64();
+          while (!mbar_test(full0 + 8 * s, (armed_par >> s) & 1u) && clock64() - t0 < WAIT_BUDGET) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // --------------------- MMA issuer (rank 0 only) ----------------------
+    if (lane == 0 && leader) {
+      int stage = 0, islot = 0;
+      uint32_t phase = 0, iphase = 0;
+      bool ok = true;
+      long long nloc = 0;
+      while (ok) {
+        if (!pair_wait(ifull0 + 8 * islot, iphase, false, abort_flag, abort_peer, P.err, 6)) break;
+        const int qidx = item_q[islot];
+        mbar_arrive_remote(iempty0_L + 8 * islot);
+        if (++islot == IQ) {
+          islot = 0;
+          iphase ^= 1;
+        }
+        if (qidx < 0) break;
+        const int4 it = P.items[qidx];
+        const int nks = P.frags[it.x].nks;
+        const int i0 = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
+        const int ntiles = (tA == tB || i0 == j) ? 1 : 2;
+        for (int t = 0; t < 2 && ok; ++t) {
+          // both CTAs' epilogues have read tile t of the previous item
+          if (nloc > 0 && !pair_wait(t == 0 ? t1empty : t2empty, (uint32_t)((nloc - 1) & 1), true,
+                                     abort_flag, abort_peer, P.err, 2)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t dL0 = tmem + (uint32_t)(t * 2 * TILE);
+          const uint32_t dL1 = dL0 + TILE;
+          for (int kc = 0; t < ntiles && kc < nks; ++kc) {
+            if (!pair_wait(full0 + 8 * stage, phase, false, abort_flag, abort_peer, P.err, 3)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sb = smem_u32(stages + stage * STAGE_BYTES);
+#pragma unroll
+            for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
+              const uint32_t koff = k16 * 32;  // bytes inside the 128-byte swizzle row
+              const uint64_t a0 = smem_desc(sb + koff);
+              const uint64_t a1 = smem_desc(sb + PANEL_BYTES + koff);
+              const uint64_t b0 = smem_desc(sb + NSL * PANEL_BYTES + koff);
+              const uint64_t b1 = smem_desc(sb + NSL * PANEL_BYTES + BPANEL_BYTES + koff);
+              const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
+              mma_f16_pair(dL0, a0, b0, acc);  // exact integer part
+              mma_f16_pair(dL1, a0, b1, acc);  // S0a R1b
+              mma_f16_pair(dL1, a1, b0, 1u);   // R1a S0b
+              mma_f16_pair(dL1, a1, b1, 1u);   // R1a R1b
+            }
+            mma_commit_pair(empty0 + 8 * stage);  // frees the stage in both CTAs
+            if (++stage == NSTAGE) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+          if (!ok) break;
+          mma_commit_pair(t == 0 ? t1full : t2full);
+        }
+        if (!ok) break;
+        ++nloc;
+      }
+      mma_commit_pair(drain);  // both CTAs learn when the last MMA has completed
+    }
+  } else {
+    // --------------------- epilogue (both CTAs) ---------------------------
+    const int ew = warp - 2;           // 0..7
+    const int quad = warp & 3;         // TMEM lane quadrant this warp may access
+    const int cbase = (ew >> 2) * 64;  // column half of the tile this warp reads
+    const int row = quad * 32 + lane;  // TMEM lane = tile row
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    int islot = 0;
+    uint32_t iphase = 0;
+    long long nloc = 0;
+    while (true) {
+      const bool w0 = pair_wait(ifull0 + 8 * islot, iphase, true, abort_flag, abort_peer, P.err, 7);
+      if (epi_any(!w0)) break;
+      const int qidx = item_q[islot];
+      __syncwarp();
+      if (lane == 0) mbar_arrive_remote(iempty0_L + 8 * islot);
+      if (++islot == IQ) {
+        islot = 0;
+        iphase ^= 1;
+      }
+      if (qidx < 0) break;
+      const int4 it = P.items[qidx];
+      const FragDesc &F = P.frags[it.x];
+      const int i0 = it.y & 0xFFFF, j = it.y >> 16, tA = it.z & 0xFFFF, tB = it.z >> 16;
+      const bool dummy = i0 + (int)rank > j;
+      const int i = dummy ? i0 : i0 + (int)rank;
+      const bool same = (i == j), diag = (tA == tB);
+      const int nvpad = F.nvpad;
+      const int a = tA * TILE + row;
+      const float *scl = P.inv_scale + F.col_base;
+      const float sa1 = scl[i * nvpad + a];                    // column (a,i)
+      const float *sbj = scl + j * nvpad + tB * TILE + cbase;  // columns (b,j)
+      const float2 *evb = P.ev2 + F.ev_off + tB * TILE + cbase;
+      // ---- T1 -> registers, then release it ----
+      const bool w1 = pair_wait(t1full, (uint32_t)(nloc & 1), false, abort_flag, abort_peer, P.err, 4);
+      if (epi_any(!w1)) break;
+      tc_fence_after();
+      const uint32_t t1 = tmem + lane_off + cbase;
+      float g1[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16) {
+        float l0[16], l1[16];
+        tmem_ld16(t1 + c0, l0);
+        tmem_ld16(t1 + TILE + c0, l1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) g1[c0 + k] = (l0[k] + l1[k]) * (sa1 * sbj[c0 + k]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive_remote(t1empty_L);
+      // ---- denominators (as split_batch_kernel) ----
+      const float2 ea = P.ev2[F.ev_off + a];
+      const float2 ei = P.eo2[F.eo_off + i], ej = P.eo2[F.eo_off + j];
+      const float sh = ei.x + ej.x;
+      const float bv = sh - ei.x;
+      const float sl = (ei.x - (sh - bv)) + (ej.x - bv) + ei.y + ej.y;
+      const float dh0 = sh - ea.x;
+      const float bw = dh0 - sh;
+      const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
+      auto terms = [&](int c0, const float *g2) -> float {
+        float ef = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const float2 eb = evb[c0 + k];
+          const float x1 = g1[c0 + k], x2 = g2[k];
+          const float dh = dh0 - eb.x;
+          const float bz = dh - dh0;
+          const float d = dh + (((dh0 - (dh - bz)) + (-eb.x - bz)) + (dl0 - eb.y));
+          const float r = rcp_denom(d);
+          const float num = diag ? x1 * fmaf(2.0f, x1, -x2) : 2.0f * fmaf(x1, x1 - x2, x2 * x2);
+          ef = fmaf(num, r, ef);
+        }
+        return ef;
+      };
+      // ---- T2' and the energy terms ----
+      const bool w2 = pair_wait(t2full, (uint32_t)(nloc & 1), false, abort_flag, abort_peer, P.err, 8);
+      if (epi_any(!w2)) break;
+      tc_fence_after();
+      double eacc = 0.0;
+      if (!dummy) {
+        if (same) {  // g_ii is symmetric
+#pragma unroll
+          for (int c0 = 0; c0 < 64; c0 += 16) {
+            float g2[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) g2[k] = g1[c0 + k];
+            eacc += (double)terms(c0, g2);
+          }
+        } else {
+          // g2(a,b) = g_ij(b,a): T1 transposed (A == B) or T2' = G_ij[B,A]
+          // transposed, through shared memory in two 64-row passes; pass h
+          // serves the warps that own columns [64h, 64h+64)
+          const uint32_t t2 = tmem + lane_off + 2 * TILE + cbase;
+          const float sbi = scl[i * nvpad + tB * TILE + row];      // T2' row (b,i)
+          const float *saj = scl + j * nvpad + tA * TILE + cbase;  // T2' columns (a,j)
+#pragma unroll 1
+          for (int h = 0; h < 2; ++h) {
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            if ((row >> 6) == h) {
+              float *dst = tbuf + (row - 64 * h) * TP + cbase;
+              if (diag) {
+#pragma unroll
+                for (int k = 0; k < 64; ++k) dst[k] = g1[k];
+              } else {
+#pragma unroll
+                for (int c0 = 0; c0 < 64; c0 += 16) {
+                  float l0[16], l1[16];
+                  tmem_ld16(t2 + c0, l0);
+                  tmem_ld16(t2 + TILE + c0, l1);
+                  tmem_wait_ld();
+#pragma unroll
+                  for (int k = 0; k < 16; ++k) dst[c0 + k] = (l0[k] + l1[k]) * (sbi * saj[c0 + k]);
+                }
+              }
+            }
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            if ((cbase >> 6) == h) {
+#pragma unroll
+              for (int c0 = 0; c0 < 64; c0 += 16) {
+                float g2[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) g2[k] = tbuf[(c0 + k) * TP + row];
+                eacc += (double)terms(c0, g2);
+              }
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive_remote(t2empty_L);
+      // reduce the item's energy over the epilogue threads
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
+      if (lane == 0) redd[ew] = eacc;
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      if (ew == 0 && lane == 0 && !dummy) {
+        double tot = 0.0;
+#pragma unroll
+        for (int w = 0; w < NEPI; ++w) tot += redd[w];
+        const long long p = (long long)j * (j + 1) / 2 + i;
+        P.part[F.item_base + p * F.ntp + it.w] = tot;
+      }
+      asm volatile("bar.sync 1, 256;" ::: "memory");
+      ++nloc;
+    }
+  }
+  __syncthreads();
+  if (warp == 1 && lane == 0) {
+    // the last MMA of the pair has completed (it may write this CTA's TMEM)
+    const long long t0 = clock64();
+    while (!mbar_test(drain, 0) && clock64() - t0 < WAIT_BUDGET) {
+    }
+  }
+  if (*abort_flag) {
+    // after an abort the peer may still have copies in flight into its own
+    // shared memory (their completion is counted in rank 0): give them time
+    // to land before either CTA exits
+    const long long t0 = clock64();
+    while (clock64() - t0 < 4000000LL) {
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync_all();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+// Pair items of a group: per fragment, for each j the i0 = 0, 2, 4, ... <= j,
+// times the tile pairs.  C(j) = number of pair items (without the tile-pair
+// factor) before column j = floor(j/2) * floor(j/2 + 1) for even j and
+// (floor(j/2) + 1)^2 for odd j.
+__host__ __device__ inline long long pair_items_before(long long j) {
+  const long long m = j / 2;
+  return (j % 2 == 0) ? m * (m + 1) : (m + 1) * (m + 1);
+}
+
+__global__ void build_pair_items_kernel(const FragDesc *__restrict__ fr, int nfrag,
+                                        long long nitems, int4 *__restrict__ items) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= nitems) return;
+  int lo = 0, hi = nfrag - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (fr[mid].pitem_base <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const FragDesc &F = fr[lo];
+  const long long loc = t - F.pitem_base;
+  const long long p2 = loc / F.ntp;
+  const int q = (int)(loc % F.ntp);
+  int j = (int)(2.0 * sqrt((double)p2));
+  if (j > F.nocc - 1) j = F.nocc - 1;
+  while (j > 0 && pair_items_before(j) > p2) --j;
+  while (j + 1 < F.nocc && pair_items_before(j + 1) <= p2) ++j;
+  const int i0 = (int)(2 * (p2 - pair_items_before(j)));
+  int tA, tB;
+  decode_tri(q, tA, tB);
+  items[t] = make_int4(lo, i0 | (j << 16), tA | (tB << 16), q);
+}
+
+// ==========================================================================
 // Local-orbital fragment energy on the tensor cores (split form):
 //   sum_ij,ab g_ij^ab / D (2 gt_ij^ab - gt_ij^ba),
 // g from Calpha C, gt from its projected copy Ct (both sliced like Calpha).
@@ -1262,13 +1821,29 @@ struct Group {
   int npairs_total = 0, max_ncol = 0, max_nv = 0;
   DevBuf frags, items, slices, inv, eo2, ev2, part, queue;
   CUtensorMap tm;
+  // paired-CTA kernel (one residual slice): its pair items and B-half map
+  bool pair = false;
+  long long npitems = 0;
+  DevBuf pitems;
+  CUtensorMap tmB;
 };
+
+// The paired-CTA kernel serves a one-residual-slice group when its dummy CTAs
+// (odd numbers of i <= j per j) add at most 4% to the group's work;
+// RIMP2_PAIR_KERNEL=0 or =1 overrides the choice (tests compare both kernels).
+bool pair_kernel_wanted(const Group &g, long long pair_slots) {
+  if (g.nsl != 2) return false;
+  const char *e = getenv("RIMP2_PAIR_KERNEL");
+  if (e && e[0] == '0') return false;
+  if (e && e[0] == '1') return true;
+  return (double)pair_slots <= 1.04 * (double)g.nitems;
+}
 
 int build_group(Group &g, cudaStream_t s) {
   // heaviest fragments first: their items lead the queue
   std::stable_sort(g.fh.begin(), g.fh.end(),
                    [](const FragDesc &x, const FragDesc &y) { return x.nks > y.nks; });
-  long long row = 0, col = 0, item = 0;
+  long long row = 0, col = 0, item = 0, pitem = 0, pair_slots = 0;
   int eo = 0, ev = 0, pb = 0;
   for (auto &F : g.fh) {
     F.nvpad = (F.nvirt + TILE - 1) / TILE * TILE;
@@ -1282,6 +1857,9 @@ int build_group(Group &g, cudaStream_t s) {
     F.row_base = row;
     F.col_base = col;
     F.item_base = item;
+    F.pitem_base = pitem;
+    pitem += pair_items_before(F.nocc) * F.ntp;
+    pair_slots += 2 * pair_items_before(F.nocc) * F.ntp;
     const int np = F.nocc * (F.nocc + 1) / 2;
     eo += F.nocc;
     ev += F.nvpad;
@@ -1294,6 +1872,7 @@ int build_group(Group &g, cudaStream_t s) {
   }
   g.nfrag = (int)g.fh.size();
   g.nitems = item;
+  g.npitems = pitem;
   g.R = row;
   g.ncol_total = col;
   g.npairs_total = pb;
@@ -1335,6 +1914,24 @@ int build_group(Group &g, cudaStream_t s) {
   auto k3 = split_batch_kernel<3, 2>;
   RIMP2_CK(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2, 3)));
   RIMP2_CK(cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(3, 2)));
+  g.pair = pair_kernel_wanted(g, pair_slots) && g.npitems <= 2147483647LL;
+  if (g.pair) {
+    RIMP2_CK(cudaFuncSetAttribute(split_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  pair_smem_bytes()));
+    cuuint32_t boxB[3] = {KSTEP, BHALF, 1};
+    cr = encode(&g.tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, g.slices.p, dims, strides, boxB, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) {
+      set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+      return RIMP2_ERR_CUDA;
+    }
+    RIMP2_TRY(g.pitems.alloc(sizeof(int4) * (size_t)g.npitems, s));
+    build_pair_items_kernel<<<(unsigned)((g.npitems + 255) / 256), 256, 0, s>>>(
+        g.frags.as<FragDesc>(), g.nfrag, g.npitems, g.pitems.as<int4>());
+    count_launch(1);
+    RIMP2_CK(cudaGetLastError());
+  }
   return RIMP2_OK;
 }
 
@@ -1369,10 +1966,24 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
     return RIMP2_ERR_CUDA;
   }
   if (ev) RIMP2_CK(cudaEventRecord(ev[1], s));
-  if (g.nsl == 2)
+  if (g.pair) {
+    PairParams Q;
+    Q.frags = fr;
+    Q.items = g.pitems.as<int4>();
+    Q.nitems = g.npitems;
+    Q.queue = P.queue;
+    Q.eo2 = P.eo2;
+    Q.ev2 = P.ev2;
+    Q.inv_scale = P.inv_scale;
+    Q.part = P.part;
+    Q.err = P.err;
+    const int npair = (int)std::min<long long>(g.npitems, std::max(1, nsm / 2));
+    split_pair_kernel<<<2 * npair, NTHREADS, pair_smem_bytes(), s>>>(g.tm, g.tmB, Q);
+  } else if (g.nsl == 2) {
     split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, P);
-  else
+  } else {
     split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, P);
+  }
   count_launch(1);
   if (ev) RIMP2_CK(cudaEventRecord(ev[2], s));
   pair_reduce_batch_kernel<<<(unsigned)((g.npairs_total + 7) / 8), 256, 0, s>>>(

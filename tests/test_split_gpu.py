@@ -135,3 +135,59 @@ def test_split_eos_identity_is_canonical():
                                 precision=api.PREC_SPLIT)
     _, E = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
     assert abs(eocc - E) <= 1e-7 * abs(E) and abs(evir - E) <= 1e-7 * abs(E)
+
+
+# (nocc, nvirt, NBA): odd and even nocc (dummy second CTA), nocc = 1, a single
+# and a ragged last virtual tile, K not a multiple of 64
+PAIR_SHAPES = [(16, 96, 384), (7, 300, 77), (1, 130, 200), (2, 128, 64), (33, 256, 1000),
+               (12, 256, 1024), (5, 17, 96)]
+
+
+@pytest.fixture
+def kernel_choice(monkeypatch):
+    def use(v):
+        monkeypatch.setenv("RIMP2_PAIR_KERNEL", v)
+    return use
+
+
+@pytest.mark.parametrize("nocc,nvirt,NBA", PAIR_SHAPES)
+def test_pair_kernel_within_1e7(api, kernel_choice, nocc, nvirt, NBA):
+    """The paired-CTA (cta_group::2) energy kernel against the FP64 oracle,
+    and against the one-CTA kernel on the same slices (one residual slice)."""
+    Ca, eo, ev = O.gen_fragment(500 + nvirt + nocc, nocc, nvirt, NBA)
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+    kernel_choice("1")
+    Ep, E = dev_energy(api, Ca, eo, ev, 1)
+    kernel_choice("0")
+    Ep1, E1 = dev_energy(api, Ca, eo, ev, 1)
+    rel = np.abs(Ep - Epr) / np.abs(Epr)
+    print(f"\npair kernel nocc={nocc} nvirt={nvirt} NBA={NBA}: pair max {rel.max():.2e} "
+          f"total {abs(E - Er) / abs(Er):.2e}; vs one-CTA {abs(E - E1) / abs(E1):.2e}")
+    bar = 1e-7 if nvirt > 1 else 2e-7
+    assert rel.max() <= bar
+    assert abs(E - Er) <= bar * abs(Er)
+    assert (np.abs(Ep - Ep1) / np.abs(Ep1)).max() <= bar
+
+
+def test_pair_kernel_batched(api, kernel_choice):
+    """Uneven fragments through one paired-CTA launch (graph-captured plan)."""
+    import torch
+    shapes = [(9, 200, 300), (16, 96, 384), (4, 257, 130), (1, 64, 64), (21, 128, 512)]
+    kernel_choice("1")
+    frags, bufs = [], []
+    for k, (nocc, nvirt, NBA) in enumerate(shapes):
+        Ca, eo, ev = O.gen_fragment(900 + k, nocc, nvirt, NBA)
+        d = [torch.from_numpy(Ca.ravel(order="F")).cuda(), torch.from_numpy(eo).cuda(),
+             torch.from_numpy(ev).cuda(), torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda"),
+             torch.zeros(1, dtype=torch.float64, device="cuda")]
+        bufs.append((Ca, eo, ev, d))
+        frags.append((nocc, nvirt, NBA) + tuple(x.data_ptr() for x in d))
+    plan = api.BatchPlan(frags, nslices=[1] * len(frags), graph=True)
+    plan.execute()
+    torch.cuda.synchronize()
+    for (nocc, nvirt, NBA), (Ca, eo, ev, d) in zip(shapes, bufs):
+        Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+        Ep = d[3].cpu().numpy().reshape(nocc, nocc, order="F")
+        assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 1e-7
+        assert abs(d[4].item() - Er) <= 1e-7 * abs(Er)
+    plan.close()
