@@ -163,15 +163,32 @@ def measured_peaks():
     return 1900.0, 1700.0, "fallback"
 
 
-def traffic_per_launch():
+def traffic_per_launch(kernel):
     """DRAM bytes per launch of the energy kernel from the committed ncu
-    capture summary (scaled to this workload), or None."""
-    p = os.path.join(ROOT, "profiles", "split_batch_kernel_traffic.json")
+    capture summary of that kernel on this workload, or None."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         d = json.load(f)
     return d.get("bytes_per_launch_full_workload")
+
+
+def performed_tiles(nocc, nvirt, paired):
+    """128x128 output tiles (over the full K) that the energy kernel computes.
+    One-CTA kernel: per i<j pair two tiles per off-diagonal tile pair and one
+    per diagonal tile pair (T2 = T1^T); per i=j pair one tile per tile pair.
+    Paired kernel: per pair item (j, i0 = 0, 2, ...) two CTAs' tiles, with one
+    product when i0 == j (the second CTA then idle) or on diagonal tile pairs."""
+    ntile = (nvirt + 127) // 128
+    ntp = ntile * (ntile + 1) // 2
+    per_pair = 2 * (ntp - ntile) + ntile
+    if not paired:
+        return nocc * (nocc - 1) // 2 * per_pair + nocc * ntp
+    m = nocc // 2
+    items = m * (m + 1) if nocc % 2 == 0 else (m + 1) ** 2
+    n_same = (nocc + 1) // 2
+    return 2 * ((items - n_same) * per_pair + n_same * ntp)
 
 
 # ------------------------------------------------------------------------------------------
@@ -483,18 +500,14 @@ def run_ours(args):
     burst, sustained, src = measured_peaks()
     kmed = statistics.median(k[1] for k in kern_ms)
     achieved = eff_flop() / (kmed * 1e-3) / 1e12
-    n_pairs_full = NOCC * (NOCC - 1) // 2
-    ntile = (NVIRT + 127) // 128
-    ntp = ntile * (ntile + 1) // 2
-    # i<j pairs: two 128x128 tiles per off-diagonal tile pair, one per diagonal
-    # tile pair (T2 = T1^T); i=j pairs: one tile per tile pair
-    tiles = n_pairs_full * (2 * (ntp - ntile) + ntile) + NOCC * ntp
+    kernel = "split_pair_kernel" if api.last_split_kernel() == 2 else "split_batch_kernel"
+    tiles = performed_tiles(NOCC, NVIRT, kernel == "split_pair_kernel")
     kpad = (NBA + 63) // 64 * 64
     performed = tiles * 128 * 128 * kpad * 2.0 * (4 if nsl == 1 else 6)
     roof = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",
-            "frac": achieved / burst, "traffic": traffic_per_launch(),
+            "frac": achieved / burst, "traffic": traffic_per_launch(kernel),
             "peak_source": f"{src} bf16_tflops (burst); fp16 kind::f16 runs at the bf16 rate",
-            "kernel": "split_batch_kernel", "kernel_ms": kmed,
+            "kernel": kernel, "kernel_ms": kmed,
             "performed_tflops": performed / (kmed * 1e-3) / 1e12,
             "performed_frac": performed / (kmed * 1e-3) / 1e12 / burst,
             "performed_frac_of_sustained": performed / (kmed * 1e-3) / 1e12 / sustained,

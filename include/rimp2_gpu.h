@@ -66,6 +66,11 @@ int rimp2_selftest_bounded_wait(long long budget_cycles, void *stream);
  * fills ms4 = {slicing, energy kernel, reductions, 0} of the last call. */
 int rimp2_set_timing(int on);
 int rimp2_last_timing(float *ms4);
+/* Energy kernel of the last split-form launch: 0 none yet, 1 one-CTA tile
+ * kernel (128x128 MMA), 2 paired-CTA kernel (cta_group::2, 256x128 MMA over
+ * two occupied pairs).  The paired kernel is opt-in: RIMP2_PAIR_KERNEL=1 in
+ * the environment selects it for one-residual-slice groups. */
+int rimp2_last_split_kernel(void);
 /* Measured FP64 tensor-op (DMMA) throughput of this GPU in TFLOP/s, the
  * denominator for the plain kernel's roofline fraction. */
 int rimp2_probe_fp64_peak(double *tflops);

@@ -31,6 +31,7 @@ SIGNATURES = {
     "rimp2_set_timing": ([C.c_int], C.c_int),
     "rimp2_selftest_bounded_wait": ([C.c_longlong, _vp], C.c_int),
     "rimp2_last_timing": ([C.POINTER(C.c_float)], C.c_int),
+    "rimp2_last_split_kernel": ([], C.c_int),
     "rimp2_probe_fp64_peak": ([_dp], C.c_int),
     "rimp2_calc_tocca": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp], C.c_int),
     "rimp2_calc_tvirta": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp], C.c_int),

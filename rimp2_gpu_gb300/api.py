@@ -394,6 +394,11 @@ def last_timing():
     return tuple(a[:3])
 
 
+def last_split_kernel():
+    """Energy kernel of the last split launch: 0 none, 1 one-CTA, 2 paired-CTA."""
+    return int(lib().rimp2_last_split_kernel())
+
+
 def probe_fp64_peak():
     """Measured FP64 DMMA throughput (TFLOP/s) of the current GPU."""
     v = C.c_double()

@@ -51,6 +51,8 @@ void set_error(const char *fmt, ...) {
 }
 void clear_error() { g_err[0] = 0; }
 void count_launch(int n) { g_launches += n; }
+static std::atomic<int> g_last_split_kernel{0};
+void note_split_kernel(int k) { g_last_split_kernel = k; }
 
 bool inject_fault(const char *what) {
   const char *v = getenv("RIMP2_FAULT_INJECT");
@@ -449,6 +451,8 @@ int rimp2_set_timing(int on) {
   g_timing = (on != 0);
   return RIMP2_OK;
 }
+
+int rimp2_last_split_kernel(void) { return g_last_split_kernel.load(); }
 
 int rimp2_last_timing(float *ms4) {
   if (!ms4) return RIMP2_ERR_ARG;

@@ -49,6 +49,7 @@
 namespace rimp2 {
 
 void count_launch(int n);
+void note_split_kernel(int k);  // 1 one-CTA, 2 paired-CTA
 __global__ void pair_reduce_kernel(const double *__restrict__ part, int nper, const int *pairs,
                                    int npairs, int nocc, double *Epair);
 __global__ void total_reduce_kernel(const double *Epair, int nocc, double *Etot);
@@ -145,6 +146,9 @@ constexpr uint32_t IDESC = (1u << 4)            // D format F32
                            | (0u << 10)         // B format F16
                            | ((uint32_t)(TILE >> 3) << 17)   // N >> 3
                            | ((uint32_t)(TILE >> 4) << 24);  // M >> 4
+
+// the same with N = 256 (two stacked 128-row B panels)
+constexpr uint32_t IDESC_N256 = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(TILE >> 4) << 24);
 
 __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
@@ -524,9 +528,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const uint32_t dst = smem_u32(stages + stage * STAGE_BYTES);
             const int rowk = (int)(F.row_base + (long long)kc * F.ncol);
 #pragma unroll
-            for (int sl = 0; sl < NSL; ++sl) {
-              tma_load_3d(dst + (2 * sl) * PANEL_BYTES, &tmap, fb, 0, rowk + colA, sl);
-              tma_load_3d(dst + (2 * sl + 1) * PANEL_BYTES, &tmap, fb, 0, rowk + colB, sl);
+            for (int sl = 0; sl < NSL; ++sl) {  // A panels, then the B panels back to back
+              tma_load_3d(dst + sl * PANEL_BYTES, &tmap, fb, 0, rowk + colA, sl);
+              tma_load_3d(dst + (NSL + sl) * PANEL_BYTES, &tmap, fb, 0, rowk + colB, sl);
             }
             if (++stage == NSTAGE) {
               stage = 0;
@@ -586,17 +590,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
               const uint32_t koff = k16 * 32;  // bytes inside the 128-byte swizzle row
               const uint64_t a0 = smem_desc(sb + 0 * PANEL_BYTES + koff);
-              const uint64_t b0 = smem_desc(sb + 1 * PANEL_BYTES + koff);
-              const uint64_t a1 = smem_desc(sb + 2 * PANEL_BYTES + koff);
-              const uint64_t b1 = smem_desc(sb + 3 * PANEL_BYTES + koff);
+              const uint64_t a1 = smem_desc(sb + 1 * PANEL_BYTES + koff);
+              const uint64_t b0 = smem_desc(sb + NSL * PANEL_BYTES + koff);
+              const uint64_t b1 = smem_desc(sb + (NSL + 1) * PANEL_BYTES + koff);
               const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
-              mma_f16(dL0, a0, b0, acc);  // exact integer part
-              mma_f16(dL1, a0, b1, acc);  // S0a R1b
-              mma_f16(dL1, a1, b0, 1u);   // R1a S0b
-              mma_f16(dL1, a1, b1, 1u);   // R1a R1b
+              // one N=256 MMA over the stacked B panels [S0b; R1b] fills
+              // [L0 | L1]: L0 += S0a S0b (exact integer part), L1 += S0a R1b
+              mma_f16_id(dL0, a0, b0, IDESC_N256, acc);
+              mma_f16(dL1, a1, b0, 1u);  // R1a S0b
+              mma_f16(dL1, a1, b1, 1u);  // R1a R1b
               if (NSL > 2) {
-                const uint64_t a2 = smem_desc(sb + 4 * PANEL_BYTES + koff);
-                const uint64_t b2 = smem_desc(sb + 5 * PANEL_BYTES + koff);
+                const uint64_t a2 = smem_desc(sb + 2 * PANEL_BYTES + koff);
+                const uint64_t b2 = smem_desc(sb + (NSL + 2) * PANEL_BYTES + koff);
                 mma_f16(dL1, a0, b2, 1u);  // S0a R2b
                 mma_f16(dL1, a2, b0, 1u);  // R2a S0b
               }
@@ -774,11 +779,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 //   T1  = G_ij[A,B] = C_iA^T C_jB   (a on the TMEM lanes, b on the columns)
 //   T2' = G_ij[B,A] = C_iB^T C_jA   (b on the lanes, a on the columns)
 // Both products of an item have the same B operand in the two CTAs (C_jB,
-// then C_jA), so each SM stages only half of it (64 rows) and its tensor core
-// reads 6 KB of shared memory per 256x128x16 step instead of the 8 KB of a
-// 128x128x16 step in split_batch_kernel; with the one-CTA tile the operand
-// reads, not the arithmetic, set the pace.  T2' is transposed through shared
-// memory in the epilogue, so that g_ij(a,b) and g_ij(b,a) meet in one thread.
+// then C_jA), which the pair splits between its shared memories.  Per K16
+// step three MMAs, as in split_batch_kernel's stacked form:
+//   256x256: S0a x [S0b; R1b] -> [L0 | L1]   (B rows 0..127 = S0b from rank 0,
+//                                             rows 128..255 = R1b from rank 1)
+//   256x128: R1a x S0b -> L1                  (64 rows of S0b from each rank)
+//   256x128: R1a x R1b -> L1                  (64 rows of R1b from each rank)
+// so each SM's tensor core reads 20 KB of operands per step where the
+// one-CTA kernel reads 28 KB, for the same 64 KB of TMA loads per stage; at
+// the GPU's power limit the smaller operand traffic is what raises the clock.
+// T2' is transposed through shared memory in the epilogue, so that g_ij(a,b)
+// and g_ij(b,a) meet in one thread.
 // A pair item with i0 + 1 > j runs its second CTA as a dummy (results
 // discarded); i0 == j (then the second CTA is a dummy) and A == B need only
 // T1.  The even CTA of the pair (rank 0) owns the work queue, the TMA full
@@ -786,11 +797,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // accumulator-empty barriers; its commits are multicast to both CTAs.  Every
 // wait is bounded; a timeout in either CTA aborts both.
 // --------------------------------------------------------------------------
-constexpr int BHALF = TILE / 2;                  // B rows staged per CTA
+constexpr int BHALF = TILE / 2;                  // B rows of an N=128 operand per CTA
 constexpr int BPANEL_BYTES = BHALF * KSTEP * 2;  // 8 KB
-constexpr int PAIR_NSTAGE = 4;
-// kind::f16, A = B = F16, D = F32, K-major, M = 256 (pair), N = 128
+constexpr int PAIR_NSTAGE = 3;
+// per-CTA stage: A panels S0a, R1a (16 KB each); Y = 128 rows of the N=256
+// operand (rank 0: S0b, rank 1: R1b); X = 64 rows of S0b; Z = 64 rows of R1b
+constexpr int PAIR_STAGE_BYTES = 3 * PANEL_BYTES + 2 * BPANEL_BYTES;  // 64 KB
+// kind::f16, A = B = F16, D = F32, K-major, M = 256 (pair), N = 128 / 256
 constexpr uint32_t IDESC_PAIR = (1u << 4) | ((uint32_t)(TILE >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+constexpr uint32_t IDESC_PAIR_N256 = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
 
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
@@ -844,12 +859,13 @@ __device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap
       : "memory");
 }
 
-__device__ __forceinline__ void mma_f16_pair(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+__device__ __forceinline__ void mma_f16_pair(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                             uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(IDESC_PAIR), "r"(acc)
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
 
@@ -905,16 +921,13 @@ struct PairParams {
   int *err;
 };
 
-int pair_smem_bytes() {
-  return PAIR_NSTAGE * 2 * (PANEL_BYTES + BPANEL_BYTES) + 1024 + 512 + 64 * TP * 4;
-}
+int pair_smem_bytes() { return PAIR_NSTAGE * PAIR_STAGE_BYTES + 1024 + 512 + 64 * TP * 4; }
 
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
     split_pair_kernel(const __grid_constant__ CUtensorMap tmA,
                       const __grid_constant__ CUtensorMap tmB, PairParams P) {
-  constexpr int NSL = 2;
   constexpr int NSTAGE = PAIR_NSTAGE;
-  constexpr int STAGE_BYTES = NSL * (PANEL_BYTES + BPANEL_BYTES);  // 48 KB per CTA
+  constexpr int STAGE_BYTES = PAIR_STAGE_BYTES;
   constexpr int NEPI = 8;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -1017,7 +1030,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
         const int ntiles = (tA == tB || i0 == j) ? 1 : 2;
         for (int t = 0; t < ntiles && ok; ++t) {
           const int colA = i * F.nvpad + (t == 0 ? tA : tB) * TILE;
-          const int colB = j * F.nvpad + (t == 0 ? tB : tA) * TILE + BHALF * (int)rank;
+          const int colB = j * F.nvpad + (t == 0 ? tB : tA) * TILE;
+          const int colH = colB + BHALF * (int)rank;  // this rank's half of the B rows
           for (int kc = 0; kc < F.nks; ++kc) {
             if (!pair_wait(empty0 + 8 * stage, phase ^ 1, false, abort_flag, abort_peer, P.err, 1)) {
               ok = false;
@@ -1031,12 +1045,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
             const uint32_t dst = smem_u32(stages + stage * STAGE_BYTES);
             const uint32_t fb = full0_L + 8 * stage;
             const int rowk = (int)(F.row_base + (long long)kc * F.ncol);
-#pragma unroll
-            for (int sl = 0; sl < NSL; ++sl) {
-              tma_load_3d_pair(dst + sl * PANEL_BYTES, &tmA, fb, 0, rowk + colA, sl);
-              tma_load_3d_pair(dst + NSL * PANEL_BYTES + sl * BPANEL_BYTES, &tmB, fb, 0,
-                               rowk + colB, sl);
-            }
+            tma_load_3d_pair(dst, &tmA, fb, 0, rowk + colA, 0);                // S0a
+            tma_load_3d_pair(dst + PANEL_BYTES, &tmA, fb, 0, rowk + colA, 1);  // R1a
+            tma_load_3d_pair(dst + 2 * PANEL_BYTES, &tmA, fb, 0, rowk + colB, (int)rank);  // Y
+            tma_load_3d_pair(dst + 3 * PANEL_BYTES, &tmB, fb, 0, rowk + colH, 0);  // X: S0b half
+            tma_load_3d_pair(dst + 3 * PANEL_BYTES + BPANEL_BYTES, &tmB, fb, 0, rowk + colH,
+                             1);  // Z: R1b half
             if (++stage == NSTAGE) {
               stage = 0;
               phase ^= 1;
@@ -1095,13 +1109,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
               const uint32_t koff = k16 * 32;  // bytes inside the 128-byte swizzle row
               const uint64_t a0 = smem_desc(sb + koff);
               const uint64_t a1 = smem_desc(sb + PANEL_BYTES + koff);
-              const uint64_t b0 = smem_desc(sb + NSL * PANEL_BYTES + koff);
-              const uint64_t b1 = smem_desc(sb + NSL * PANEL_BYTES + BPANEL_BYTES + koff);
+              const uint64_t by = smem_desc(sb + 2 * PANEL_BYTES + koff);
+              const uint64_t bx = smem_desc(sb + 3 * PANEL_BYTES + koff);
+              const uint64_t bz = smem_desc(sb + 3 * PANEL_BYTES + BPANEL_BYTES + koff);
               const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
-              mma_f16_pair(dL0, a0, b0, acc);  // exact integer part
-              mma_f16_pair(dL1, a0, b1, acc);  // S0a R1b
-              mma_f16_pair(dL1, a1, b0, 1u);   // R1a S0b
-              mma_f16_pair(dL1, a1, b1, 1u);   // R1a R1b
+              // [L0 | L1] += S0a x [S0b; R1b]: exact integer part and S0a R1b
+              mma_f16_pair(dL0, a0, by, IDESC_PAIR_N256, acc);
+              mma_f16_pair(dL1, a1, bx, IDESC_PAIR, 1u);  // R1a S0b
+              mma_f16_pair(dL1, a1, bz, IDESC_PAIR, 1u);  // R1a R1b
             }
             mma_commit_pair(empty0 + 8 * stage);  // frees the stage in both CTAs
             if (++stage == NSTAGE) {
@@ -1485,6 +1500,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // ------------------------------ MMA issuer --------------------------------
     if (lane == 0) {
       constexpr uint32_t idesc = (IDESC & ~(0x3Fu << 17)) | ((uint32_t)(HALF >> 3) << 17);
+      // N = 128: the two adjacent 64-row B panels [S0b; R1b] at once
+      constexpr uint32_t idesc2 = IDESC;
       int stage = 0, islot = 0;
       uint32_t phase = 0, iphase = 0;
       bool ok = true;
@@ -1529,8 +1546,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint64_t b0 = smem_desc(sbB + 0 * HPANEL_BYTES + koff);
               const uint64_t b1 = smem_desc(sbB + 1 * HPANEL_BYTES + koff);
               const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
-              mma_f16_id(dL0, a0, b0, idesc, acc);  // exact integer part
-              mma_f16_id(dL1, a0, b1, idesc, acc);  // S0a R1b
+              // [L0 | L1] += S0a x [S0b; R1b]: exact integer part and S0a R1b
+              mma_f16_id(dL0, a0, b0, idesc2, acc);
               mma_f16_id(dL1, a1, b0, idesc, 1u);   // R1a S0b
               mma_f16_id(dL1, a1, b1, idesc, 1u);   // R1a R1b
               if (NSL > 2) {
@@ -1828,22 +1845,21 @@ struct Group {
   CUtensorMap tmB;
 };
 
-// The paired-CTA kernel serves a one-residual-slice group when its dummy CTAs
-// (odd numbers of i <= j per j) add at most 4% to the group's work;
-// RIMP2_PAIR_KERNEL=0 or =1 overrides the choice (tests compare both kernels).
-bool pair_kernel_wanted(const Group &g, long long pair_slots) {
+// The paired-CTA kernel is opt-in (RIMP2_PAIR_KERNEL=1, one-residual-slice
+// groups only): on the nocc=128 nvirt=1024 NBA=4096 fragment it measured 2.4%
+// slower than the one-CTA kernel with the stacked N=256 MMA (165.7 vs 161.1 ms
+// at the same power-capped clock), so the one-CTA kernel is the default.
+bool pair_kernel_wanted(const Group &g) {
   if (g.nsl != 2) return false;
   const char *e = getenv("RIMP2_PAIR_KERNEL");
-  if (e && e[0] == '0') return false;
-  if (e && e[0] == '1') return true;
-  return (double)pair_slots <= 1.04 * (double)g.nitems;
+  return e && e[0] == '1';
 }
 
 int build_group(Group &g, cudaStream_t s) {
   // heaviest fragments first: their items lead the queue
   std::stable_sort(g.fh.begin(), g.fh.end(),
                    [](const FragDesc &x, const FragDesc &y) { return x.nks > y.nks; });
-  long long row = 0, col = 0, item = 0, pitem = 0, pair_slots = 0;
+  long long row = 0, col = 0, item = 0, pitem = 0;
   int eo = 0, ev = 0, pb = 0;
   for (auto &F : g.fh) {
     F.nvpad = (F.nvirt + TILE - 1) / TILE * TILE;
@@ -1859,7 +1875,6 @@ int build_group(Group &g, cudaStream_t s) {
     F.item_base = item;
     F.pitem_base = pitem;
     pitem += pair_items_before(F.nocc) * F.ntp;
-    pair_slots += 2 * pair_items_before(F.nocc) * F.ntp;
     const int np = F.nocc * (F.nocc + 1) / 2;
     eo += F.nocc;
     ev += F.nvpad;
@@ -1914,7 +1929,7 @@ int build_group(Group &g, cudaStream_t s) {
   auto k3 = split_batch_kernel<3, 2>;
   RIMP2_CK(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2, 3)));
   RIMP2_CK(cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(3, 2)));
-  g.pair = pair_kernel_wanted(g, pair_slots) && g.npitems <= 2147483647LL;
+  g.pair = pair_kernel_wanted(g) && g.npitems <= 2147483647LL;
   if (g.pair) {
     RIMP2_CK(cudaFuncSetAttribute(split_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   pair_smem_bytes()));
@@ -1979,9 +1994,12 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
     Q.err = P.err;
     const int npair = (int)std::min<long long>(g.npitems, std::max(1, nsm / 2));
     split_pair_kernel<<<2 * npair, NTHREADS, pair_smem_bytes(), s>>>(g.tm, g.tmB, Q);
+    note_split_kernel(2);
   } else if (g.nsl == 2) {
+    note_split_kernel(1);
     split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, P);
   } else {
+    note_split_kernel(1);
     split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, P);
   }
   count_launch(1);
@@ -2513,6 +2531,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
     }
     BP.queue = g.queue.as<unsigned int>();
     const int grid = (int)std::min<long long>(BP.nitems - BP.item_begin, P->nsm);
+    note_split_kernel(1);
     if (g.nsl == 2)
       split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, BP);
     else

@@ -38,3 +38,20 @@ def test_workload_generators_and_flop_count():
     # 2 NBA (nocc nvirt)^2 at the large fragment
     assert bench.eff_flop(128, 1024, 4096) == 2.0 * 4096 * (128 * 1024) ** 2
     assert abs(bench.eff_flop(128, 1024, 4096) - 1.407e14) / 1.407e14 < 1e-3
+
+
+def test_performed_tiles_match_enumeration():
+    """The performed-work count of both energy kernels against an explicit
+    enumeration of their work items."""
+    sys.path.insert(0, ROOT)
+    import bench
+    for nocc in (1, 2, 5, 8, 33, 128):
+        for nvirt in (1, 96, 128, 300, 1024):
+            nt = (nvirt + 127) // 128
+            tps = [(a, b) for b in range(nt) for a in range(b + 1)]
+            one = sum(1 if (i == j or a == b) else 2
+                      for j in range(nocc) for i in range(j + 1) for a, b in tps)
+            pair = sum(2 * (1 if (a == b or i0 == j) else 2)
+                       for j in range(nocc) for i0 in range(0, j + 1, 2) for a, b in tps)
+            assert bench.performed_tiles(nocc, nvirt, False) == one
+            assert bench.performed_tiles(nocc, nvirt, True) == pair
