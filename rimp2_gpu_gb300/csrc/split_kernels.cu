@@ -112,6 +112,22 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
   return true;
 }
 
+// OR of a predicate over the 256 epilogue threads (named barrier 1).  The
+// epilogue warps leave their loop together on a failed bounded wait, so that
+// none is left waiting at a later named barrier for a warp that has gone.
+__device__ __forceinline__ bool epi_any(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, o;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred o, 1, 256, q;\n\t"
+      "selp.u32 %0, 1, 0, o;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p)
+      : "memory");
+  return r != 0;
+}
+
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, uint32_t bar,
                                             int c0, int c1, int c2) {
   asm volatile(
@@ -635,7 +651,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint32_t iphase = 0;
     long long nloc = 0;
     while (true) {
-      if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7)) break;
+      const bool w0 = mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7);
+      if (epi_any(!w0)) break;
       const int qidx = item_q[islot];
       __syncwarp();
       if (lane == 0) mbar_arrive(iempty0 + 8 * islot);
@@ -657,7 +674,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float *sbi = scl + i * nvpad + tB * TILE + cbase;
       const float2 *evb = P.ev2 + F.ev_off + tB * TILE + cbase;
       // ---- T1 -> registers, then hand its TMEM back to the MMA issuer ----
-      if (!mbar_wait(t1full, (uint32_t)(nloc & 1), abort_flag, P.err, 4)) break;
+      const bool w1 = mbar_wait(t1full, (uint32_t)(nloc & 1), abort_flag, P.err, 4);
+      if (epi_any(!w1)) break;
       tc_fence_after();
       const uint32_t t1 = tmem + lane_off + cbase;
       float g1[64];
@@ -685,7 +703,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float bw = dh0 - sh;
       const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
       // ---- T2 and the energy terms ----
-      if (!mbar_wait(t2full, (uint32_t)(nloc & 1), abort_flag, P.err, 8)) break;
+      const bool w2 = mbar_wait(t2full, (uint32_t)(nloc & 1), abort_flag, P.err, 8);
+      if (epi_any(!w2)) break;
       tc_fence_after();
       const uint32_t t2 = tmem + lane_off + 2 * TILE + cbase;
       // one 16-column chunk of energy terms, g2 supplied by `g2at(k)`
@@ -877,20 +896,6 @@ __device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
       " [%0], %1;" ::"r"(bar),
       "h"((uint16_t)3)
       : "memory");
-}
-
-// OR of a predicate over the 256 epilogue threads (named barrier 1)
-__device__ __forceinline__ bool epi_any(bool p) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred q, o;\n\t"
-      "setp.ne.u32 q, %1, 0;\n\t"
-      "bar.red.or.pred o, 1, 256, q;\n\t"
-      "selp.u32 %0, 1, 0, o;\n\t}"
-      : "=r"(r)
-      : "r"((uint32_t)p)
-      : "memory");
-  return r != 0;
 }
 
 // Bounded wait that also aborts the peer CTA on a timeout.
@@ -1590,7 +1595,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     uint32_t par = 0;  // per tile: parity of the reads so far
     bool ok = true;
     while (ok) {
-      if (!mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7)) break;
+      const bool w0 = mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7);
+      if (epi_any(!w0)) break;
       const long long qidx = item_q[islot];
       __syncwarp();
       if (lane == 0) mbar_arrive(iempty0 + 8 * islot);
@@ -1617,7 +1623,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
       // one tile's 32 columns of this thread into registers, then release it
       auto take = [&](int t, const float *sr, float srow, float (&v)[32]) -> bool {
-        if (!mbar_wait(tfull0 + 8 * t, (par >> t) & 1, abort_flag, P.err, 4)) return false;
+        const bool w = mbar_wait(tfull0 + 8 * t, (par >> t) & 1, abort_flag, P.err, 4);
+        if (epi_any(!w)) return false;
         tc_fence_after();
 #pragma unroll
         for (int c0 = 0; c0 < 32; c0 += 16) {
