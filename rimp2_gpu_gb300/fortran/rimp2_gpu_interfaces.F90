@@ -184,6 +184,11 @@ module rimp2_gpu_interfaces
        type(C_PTR), value :: stream
      end function rimp2_set_stream
 
+     ! energy kernel of the last split launch: 0 none, 1 one-CTA, 2 paired-CTA
+     integer(C_INT) function rimp2_last_split_kernel() bind(C, name="rimp2_last_split_kernel")
+       import :: C_INT
+     end function rimp2_last_split_kernel
+
      ! C string of the last error on this thread
      type(C_PTR) function rimp2_last_error_string() bind(C, name="rimp2_last_error_string")
        import :: C_PTR

@@ -191,3 +191,17 @@ def test_pair_kernel_batched(api, kernel_choice):
         assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 1e-7
         assert abs(d[4].item() - Er) <= 1e-7 * abs(Er)
     plan.close()
+
+
+def test_kernel_choice_is_reported(api, kernel_choice):
+    """The split form runs the one-CTA kernel unless the paired one is asked
+    for, and the library says which kernel ran."""
+    Ca, eo, ev = O.gen_fragment(31, 6, 200, 256)
+    kernel_choice("")
+    dev_energy(api, Ca, eo, ev, 1)
+    assert api.last_split_kernel() == 1
+    kernel_choice("1")
+    dev_energy(api, Ca, eo, ev, 1)
+    assert api.last_split_kernel() == 2
+    dev_energy(api, Ca, eo, ev, 2)  # two residual slices: one-CTA kernel only
+    assert api.last_split_kernel() == 1
