@@ -503,7 +503,10 @@ def run_ours(args):
     kernel = "split_pair_kernel" if api.last_split_kernel() == 2 else "split_batch_kernel"
     tiles = performed_tiles(NOCC, NVIRT, kernel == "split_pair_kernel")
     kpad = (NBA + 63) // 64 * 64
-    performed = tiles * 128 * 128 * kpad * 2.0 * (4 if nsl == 1 else 6)
+    # products per element pair: 4 (S0S0, S0R1, R1S0, R1R1) with one residual
+    # slice, 6 with two; the paired kernel folds the two R1a terms into R1a V
+    products = 3 if kernel == "split_pair_kernel" else (4 if nsl == 1 else 6)
+    performed = tiles * 128 * 128 * kpad * 2.0 * products
     roof = {"bound": "tensor", "achieved": achieved, "peak": burst, "unit": "TFLOP/s",
             "frac": achieved / burst, "traffic": traffic_per_launch(kernel),
             "peak_source": f"{src} bf16_tflops (burst); fp16 kind::f16 runs at the bf16 rate",

@@ -309,7 +309,8 @@ __device__ __forceinline__ void decode_pair(int p, int &i, int &j) {
 // grid.y = fragment, one warp per column.
 __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, long long plane,
                                    __half *__restrict__ slices, float *__restrict__ inv_scale,
-                                   int col0, int col1) {
+                                   int col0, int col1, int vplane = 0,
+                                   float *__restrict__ dcorr = nullptr) {
   // columns [col0, min(col1, ncol)) of each fragment
   const FragDesc &F = fr[blockIdx.y];
   const int col = col0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -323,9 +324,12 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
   if (a >= F.nvirt) {
     for (int k = lane; k < Kpad; k += 32) {
       const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
-      for (int sl = 0; sl < nsl; ++sl) out[sl * plane + o] = hz;
+      for (int sl = 0; sl < nsl + vplane; ++sl) out[sl * plane + o] = hz;
     }
-    if (lane == 0) inv_scale[F.col_base + col] = 1.0f;
+    if (lane == 0) {
+      inv_scale[F.col_base + col] = 1.0f;
+      if (vplane) dcorr[F.col_base + col] = 0.0f;
+    }
     return;
   }
   const int NBA = F.NBA;
@@ -362,8 +366,10 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
     e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
     e = max(-100, min(100, e));
   }
+  if (vplane && lane == 0) dcorr[F.col_base + col] = 0.0f;
   for (int attempt = 0; attempt < 64; ++attempt) {
     long long n2 = 0;  // sum of S0^2 (integers; <= 2^24 is the test)
+    float dsum = 0.0f;  // sum of R1 (V - S0 - R1) (V plane only)
     for (int k0 = lane; k0 < Kpad; k0 += 128) {
       double v[4];
 #pragma unroll
@@ -372,7 +378,7 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
       for (int u = 0; u < 4; ++u) {
         const int k = k0 + 32 * u;
         if (k >= Kpad) break;
-        __half h0 = hz, h1 = hz, h2 = hz;
+        __half h0 = hz, h1 = hz, h2 = hz, hv = hz;
         if (k < NBA) {
           float xh, xl;
           split_double(v[u], e, xh, xl);
@@ -383,16 +389,30 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
           h2 = __float2half_rn(r - __half2float(h1));
           const int qi = (int)q;
           n2 += (long long)qi * qi;
+          if (vplane) {
+            // V = C*s in FP16; its rounding error against S0 + R1 is exact in FP32
+            hv = __float2half_rn(q + r);
+            const float r1 = __half2float(h1);
+            dsum = fmaf(r1, (__half2float(hv) - q) - r1, dsum);
+          }
         }
         const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
         out[o] = h0;
         if (nsl > 1) out[plane + o] = h1;
         if (nsl > 2) out[2 * plane + o] = h2;
+        if (vplane) out[nsl * plane + o] = hv;
       }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
-    if (n2 <= 16777216LL) break;  // ||S0||^2 <= 2^24: L0 accumulation exact
+    if (n2 <= 16777216LL) {  // ||S0||^2 <= 2^24: L0 accumulation exact
+      if (vplane) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        if (lane == 0) dcorr[F.col_base + col] = dsum;
+      }
+      break;
+    }
     --e;
   }
   if (lane == 0) inv_scale[F.col_base + col] = ldexpf(1.0f, -e);
@@ -798,15 +818,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 //   T1  = G_ij[A,B] = C_iA^T C_jB   (a on the TMEM lanes, b on the columns)
 //   T2' = G_ij[B,A] = C_iB^T C_jA   (b on the lanes, a on the columns)
 // Both products of an item have the same B operand in the two CTAs (C_jB,
-// then C_jA), which the pair splits between its shared memories.  Per K16
-// step three MMAs, as in split_batch_kernel's stacked form:
+// then C_jA), which the pair splits between its shared memories.  This
+// kernel uses a third slice plane V = fp16(C*s) and folds the two R1a terms
+// into one product, R1a S0b + R1a R1b = R1a V - R1a (V - S0 - R1), so a K16
+// step is two MMAs (three products instead of four):
 //   256x256: S0a x [S0b; R1b] -> [L0 | L1]   (B rows 0..127 = S0b from rank 0,
 //                                             rows 128..255 = R1b from rank 1)
-//   256x128: R1a x S0b -> L1                  (64 rows of S0b from each rank)
-//   256x128: R1a x R1b -> L1                  (64 rows of R1b from each rank)
-// so each SM's tensor core reads 20 KB of operands per step where the
-// one-CTA kernel reads 28 KB, for the same 64 KB of TMA loads per stage; at
-// the GPU's power limit the smaller operand traffic is what raises the clock.
+//   256x128: R1a x Vb -> L1                   (64 rows of V from each rank)
+// The dropped term sum_k R1a (Vb - S0b - R1b) is a product of two
+// independent rounding residues for distinct columns (a,i) != (b,j), an
+// unbiased error of ~2^-21 of g that averages out of the pair energies; for
+// the same column it is a sum of R1 times its own rounding error, a bias,
+// which the slicing kernel computes per column (dcorr) and the epilogue
+// subtracts from g_ii(a,a).  Each SM's tensor core reads 14 KB of operands
+// per step (the one-CTA kernel: 28 KB for four products).
 // T2' is transposed through shared memory in the epilogue, so that g_ij(a,b)
 // and g_ij(b,a) meet in one thread.
 // A pair item with i0 + 1 > j runs its second CTA as a dummy (results
@@ -820,8 +845,8 @@ constexpr int BHALF = TILE / 2;                  // B rows of an N=128 operand p
 constexpr int BPANEL_BYTES = BHALF * KSTEP * 2;  // 8 KB
 constexpr int PAIR_NSTAGE = 3;
 // per-CTA stage: A panels S0a, R1a (16 KB each); Y = 128 rows of the N=256
-// operand (rank 0: S0b, rank 1: R1b); X = 64 rows of S0b; Z = 64 rows of R1b
-constexpr int PAIR_STAGE_BYTES = 3 * PANEL_BYTES + 2 * BPANEL_BYTES;  // 64 KB
+// operand (rank 0: S0b, rank 1: R1b); W = 64 rows of Vb
+constexpr int PAIR_STAGE_BYTES = 3 * PANEL_BYTES + BPANEL_BYTES;  // 56 KB
 // kind::f16, A = B = F16, D = F32, K-major, M = 256 (pair), N = 128 / 256
 constexpr uint32_t IDESC_PAIR = (1u << 4) | ((uint32_t)(TILE >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
 constexpr uint32_t IDESC_PAIR_N256 = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
@@ -918,7 +943,9 @@ __device__ __forceinline__ bool pair_wait(uint32_t bar, uint32_t parity, bool cl
 struct PairParams {
   const FragDesc *frags;
   const int4 *items;     // {fragment, i0 | j << 16, tA | tB << 16, tile pair index}
-  long long nitems;
+  long long nitems;      // this launch drains items [item_begin, nitems)
+  long long item_begin;
+  const float *dcorr;    // per column: sum over K of R1 (V - S0 - R1)
   unsigned int *queue;   // next item counter (reset per launch)
   const float2 *eo2, *ev2;
   const float *inv_scale;
@@ -1011,7 +1038,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
         if (leader) {
           if (!pair_wait(iempty0 + 8 * islot, iphase ^ 1, true, abort_flag, abort_peer, P.err, 5))
             break;
-          const long long id = (long long)atomicAdd(P.queue, 1u);
+          const long long id = P.item_begin + (long long)atomicAdd(P.queue, 1u);
           qidx = id < P.nitems ? (int)id : -1;
           item_q[islot] = qidx;
           st_remote_u32(item_q_peer + 4 * islot, (uint32_t)qidx);
@@ -1053,9 +1080,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
             tma_load_3d_pair(dst, &tmA, fb, 0, rowk + colA, 0);                // S0a
             tma_load_3d_pair(dst + PANEL_BYTES, &tmA, fb, 0, rowk + colA, 1);  // R1a
             tma_load_3d_pair(dst + 2 * PANEL_BYTES, &tmA, fb, 0, rowk + colB, (int)rank);  // Y
-            tma_load_3d_pair(dst + 3 * PANEL_BYTES, &tmB, fb, 0, rowk + colH, 0);  // X: S0b half
-            tma_load_3d_pair(dst + 3 * PANEL_BYTES + BPANEL_BYTES, &tmB, fb, 0, rowk + colH,
-                             1);  // Z: R1b half
+            tma_load_3d_pair(dst + 3 * PANEL_BYTES, &tmB, fb, 0, rowk + colH, 2);  // W: V half
             if (++stage == NSTAGE) {
               stage = 0;
               phase ^= 1;
@@ -1115,13 +1140,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
               const uint64_t a0 = smem_desc(sb + koff);
               const uint64_t a1 = smem_desc(sb + PANEL_BYTES + koff);
               const uint64_t by = smem_desc(sb + 2 * PANEL_BYTES + koff);
-              const uint64_t bx = smem_desc(sb + 3 * PANEL_BYTES + koff);
-              const uint64_t bz = smem_desc(sb + 3 * PANEL_BYTES + BPANEL_BYTES + koff);
+              const uint64_t bw = smem_desc(sb + 3 * PANEL_BYTES + koff);
               const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
               // [L0 | L1] += S0a x [S0b; R1b]: exact integer part and S0a R1b
               mma_f16_pair(dL0, a0, by, IDESC_PAIR_N256, acc);
-              mma_f16_pair(dL1, a1, bx, IDESC_PAIR, 1u);  // R1a S0b
-              mma_f16_pair(dL1, a1, bz, IDESC_PAIR, 1u);  // R1a R1b
+              mma_f16_pair(dL1, a1, bw, IDESC_PAIR, 1u);  // R1a V = R1a (S0b + R1b) + ...
             }
             mma_commit_pair(empty0 + 8 * stage);  // frees the stage in both CTAs
             if (++stage == NSTAGE) {
@@ -1188,6 +1211,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive_remote(t1empty_L);
+      if (same && diag && !dummy) {
+        // g_ii(a,a): remove the same-column bias of the folded R1 V product
+        const float corr = P.dcorr[F.col_base + i * nvpad + a] * (sa1 * sa1);
+        const int kd = row - cbase;  // this row's diagonal element in the warp's column half
+#pragma unroll
+        for (int k = 0; k < 64; ++k)
+          if (k == kd) g1[k] -= corr;
+      }
       // ---- denominators (as split_batch_kernel) ----
       const float2 ea = P.ev2[F.ev_off + a];
       const float2 ei = P.eo2[F.eo_off + i], ej = P.eo2[F.eo_off + j];
@@ -1847,19 +1878,22 @@ struct Group {
   CUtensorMap tm;
   // paired-CTA kernel (one residual slice): its pair items and B-half map
   bool pair = false;
-  long long npitems = 0;
-  DevBuf pitems;
+  long long npitems = 0, pair_slots = 0;
+  DevBuf pitems, dcorr;  // dcorr: per-column diagonal correction of the V product
   CUtensorMap tmB;
 };
 
-// The paired-CTA kernel is opt-in (RIMP2_PAIR_KERNEL=1, one-residual-slice
-// groups only): on the nocc=128 nvirt=1024 NBA=4096 fragment it measured 2.4%
-// slower than the one-CTA kernel with the stacked N=256 MMA (165.7 vs 161.1 ms
-// at the same power-capped clock), so the one-CTA kernel is the default.
+// A one-residual-slice group runs the paired-CTA kernel (three products per
+// element pair, 0.87x the one-CTA kernel's time on the nocc=128 nvirt=1024
+// NBA=4096 fragment) unless its dummy CTAs (an odd count of i <= j for some
+// j) add more than 10% to the work: at nocc = 8 they add 11%, at 16 5.9%.
+// RIMP2_PAIR_KERNEL=0 or =1 overrides the choice.
 bool pair_kernel_wanted(const Group &g) {
   if (g.nsl != 2) return false;
   const char *e = getenv("RIMP2_PAIR_KERNEL");
-  return e && e[0] == '1';
+  if (e && e[0] == '0') return false;
+  if (e && e[0] == '1') return true;
+  return (double)g.pair_slots <= 1.10 * (double)g.nitems;
 }
 
 int build_group(Group &g, cudaStream_t s) {
@@ -1882,6 +1916,7 @@ int build_group(Group &g, cudaStream_t s) {
     F.item_base = item;
     F.pitem_base = pitem;
     pitem += pair_items_before(F.nocc) * F.ntp;
+    g.pair_slots += 2 * pair_items_before(F.nocc) * F.ntp;
     const int np = F.nocc * (F.nocc + 1) / 2;
     eo += F.nocc;
     ev += F.nvpad;
@@ -1902,10 +1937,13 @@ int build_group(Group &g, cudaStream_t s) {
     set_error("split batch too large for one launch (rows=%lld, items=%lld)", g.R, g.nitems);
     return RIMP2_ERR_ARG;
   }
+  g.pair = pair_kernel_wanted(g) && g.npitems <= 2147483647LL;
+  const int planes = g.nsl + (g.pair ? 1 : 0);  // the paired kernel adds the V plane
   RIMP2_TRY(g.frags.alloc(sizeof(FragDesc) * g.nfrag, s));
   RIMP2_TRY(g.items.alloc(sizeof(int4) * (size_t)g.nitems, s));
-  RIMP2_TRY(g.slices.alloc(sizeof(__half) * (size_t)g.nsl * (size_t)g.R * 64, s));
+  RIMP2_TRY(g.slices.alloc(sizeof(__half) * (size_t)planes * (size_t)g.R * 64, s));
   RIMP2_TRY(g.inv.alloc(sizeof(float) * (size_t)g.ncol_total, s));
+  if (g.pair) RIMP2_TRY(g.dcorr.alloc(sizeof(float) * (size_t)g.ncol_total, s));
   RIMP2_TRY(g.eo2.alloc(sizeof(float2) * (size_t)eo, s));
   RIMP2_TRY(g.ev2.alloc(sizeof(float2) * (size_t)ev, s));
   RIMP2_TRY(g.part.alloc(sizeof(double) * (size_t)g.nitems, s));
@@ -1921,7 +1959,7 @@ int build_group(Group &g, cudaStream_t s) {
     set_error("cuTensorMapEncodeTiled entry point unavailable");
     return RIMP2_ERR_UNSUPPORTED;
   }
-  cuuint64_t dims[3] = {64, (cuuint64_t)g.R, (cuuint64_t)g.nsl};
+  cuuint64_t dims[3] = {64, (cuuint64_t)g.R, (cuuint64_t)planes};
   cuuint64_t strides[2] = {128, (cuuint64_t)g.R * 128};
   cuuint32_t box[3] = {KSTEP, TILE, 1};
   cuuint32_t estr[3] = {1, 1, 1};
@@ -1936,7 +1974,6 @@ int build_group(Group &g, cudaStream_t s) {
   auto k3 = split_batch_kernel<3, 2>;
   RIMP2_CK(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2, 3)));
   RIMP2_CK(cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(3, 2)));
-  g.pair = pair_kernel_wanted(g) && g.npitems <= 2147483647LL;
   if (g.pair) {
     RIMP2_CK(cudaFuncSetAttribute(split_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   pair_smem_bytes()));
@@ -1965,7 +2002,8 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
   {
     dim3 grid((unsigned)((g.max_ncol * 32LL + 255) / 256), (unsigned)g.nfrag);
     slice_batch_kernel<<<grid, 256, 0, s>>>(fr, g.nsl, g.R * 64, g.slices.as<__half>(),
-                                            g.inv.as<float>(), 0, 0x7fffffff);
+                                            g.inv.as<float>(), 0, 0x7fffffff, g.pair ? 1 : 0,
+                                            g.dcorr.as<float>());
     dim3 g2((unsigned)((g.max_nv + 255) / 256), (unsigned)g.nfrag);
     eps_batch_kernel<<<g2, 256, 0, s>>>(fr, g.eo2.as<float2>(), g.ev2.as<float2>());
     count_launch(2);
@@ -1993,6 +2031,8 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
     Q.frags = fr;
     Q.items = g.pitems.as<int4>();
     Q.nitems = g.npitems;
+    Q.item_begin = 0;
+    Q.dcorr = g.dcorr.as<float>();
     Q.queue = P.queue;
     Q.eo2 = P.eo2;
     Q.ev2 = P.ev2;
@@ -2525,24 +2565,44 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
     }
     const int col0 = i0 * F.nvpad, col1 = i1 * F.nvpad;
     slice_batch_kernel<<<(unsigned)(((long long)(col1 - col0) * 32 + 255) / 256), 256, 0, s>>>(
-        fr, g.nsl, g.R * 64, g.slices.as<__half>(), g.inv.as<float>(), col0, col1);
-    // pairs (i<=j) with j in [i0, i1): pair indices [i0(i0+1)/2, i1(i1+1)/2)
-    const long long pb = (long long)i0 * (i0 + 1) / 2, pe = (long long)i1 * (i1 + 1) / 2;
-    BP.item_begin = pb * F.ntp;
-    BP.nitems = pe * F.ntp;
+        fr, g.nsl, g.R * 64, g.slices.as<__half>(), g.inv.as<float>(), col0, col1,
+        g.pair ? 1 : 0, g.dcorr.as<float>());
     e = cudaMemsetAsync(g.queue.p, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) {
       set_error("queue reset failed: %s", cudaGetErrorString(e));
       rc = RIMP2_ERR_CUDA;
       break;
     }
-    BP.queue = g.queue.as<unsigned int>();
-    const int grid = (int)std::min<long long>(BP.nitems - BP.item_begin, P->nsm);
-    note_split_kernel(1);
-    if (g.nsl == 2)
-      split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, BP);
-    else
-      split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, BP);
+    if (g.pair) {
+      // pair items with j in [i0, i1) (their i0' < i0'+1 <= j are already copied)
+      PairParams Q;
+      Q.frags = fr;
+      Q.items = g.pitems.as<int4>();
+      Q.item_begin = pair_items_before(i0) * F.ntp;
+      Q.nitems = pair_items_before(i1) * F.ntp;
+      Q.dcorr = g.dcorr.as<float>();
+      Q.queue = g.queue.as<unsigned int>();
+      Q.eo2 = BP.eo2;
+      Q.ev2 = BP.ev2;
+      Q.inv_scale = BP.inv_scale;
+      Q.part = BP.part;
+      Q.err = BP.err;
+      const int npair = (int)std::min<long long>(Q.nitems - Q.item_begin, std::max(1, P->nsm / 2));
+      note_split_kernel(2);
+      split_pair_kernel<<<2 * npair, NTHREADS, pair_smem_bytes(), s>>>(g.tm, g.tmB, Q);
+    } else {
+      // pairs (i<=j) with j in [i0, i1): pair indices [i0(i0+1)/2, i1(i1+1)/2)
+      const long long pb = (long long)i0 * (i0 + 1) / 2, pe = (long long)i1 * (i1 + 1) / 2;
+      BP.item_begin = pb * F.ntp;
+      BP.nitems = pe * F.ntp;
+      BP.queue = g.queue.as<unsigned int>();
+      const int grid = (int)std::min<long long>(BP.nitems - BP.item_begin, P->nsm);
+      note_split_kernel(1);
+      if (g.nsl == 2)
+        split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, BP);
+      else
+        split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, BP);
+    }
     count_launch(2);
     e = cudaGetLastError();
     if (e != cudaSuccess) {

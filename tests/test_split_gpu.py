@@ -194,14 +194,34 @@ def test_pair_kernel_batched(api, kernel_choice):
 
 
 def test_kernel_choice_is_reported(api, kernel_choice):
-    """The split form runs the one-CTA kernel unless the paired one is asked
-    for, and the library says which kernel ran."""
-    Ca, eo, ev = O.gen_fragment(31, 6, 200, 256)
+    """One-residual-slice fragments run the paired kernel unless its dummy
+    CTAs would add more than 10% work (nocc = 6: 14%, nocc = 32: 3%); the
+    environment overrides the choice and the library says which kernel ran."""
+    small = O.gen_fragment(31, 6, 200, 256)
+    big = O.gen_fragment(32, 32, 130, 128)
     kernel_choice("")
-    dev_energy(api, Ca, eo, ev, 1)
+    dev_energy(api, *small, 1)
+    assert api.last_split_kernel() == 1
+    dev_energy(api, *big, 1)
+    assert api.last_split_kernel() == 2
+    kernel_choice("0")
+    dev_energy(api, *big, 1)
     assert api.last_split_kernel() == 1
     kernel_choice("1")
-    dev_energy(api, Ca, eo, ev, 1)
+    dev_energy(api, *small, 1)
     assert api.last_split_kernel() == 2
-    dev_energy(api, Ca, eo, ev, 2)  # two residual slices: one-CTA kernel only
+    dev_energy(api, *small, 2)  # two residual slices: one-CTA kernel only
     assert api.last_split_kernel() == 1
+
+
+@pytest.mark.parametrize("nocc,nvirt,NBA", [(33, 256, 1000), (9, 130, 512)])
+def test_pair_kernel_host_streamed(api, kernel_choice, nocc, nvirt, NBA):
+    """The host-pointer split call copies Calpha in occupied chunks and runs
+    the paired kernel on each chunk's pair items as the chunk lands."""
+    Ca, eo, ev = O.gen_fragment(700 + nocc, nocc, nvirt, NBA)
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+    kernel_choice("1")
+    Ep, E = api.energy(nvirt, nocc, NBA, Ca, eo, ev, precision=api.PREC_SPLIT)
+    assert api.last_split_kernel() == 2
+    assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 1e-7
+    assert abs(E - Er) <= 1e-7 * abs(Er)
