@@ -947,7 +947,7 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
 // Default = the table measured by rimp2_gpu_gb300/autotune.py on GB300 with a
 // 2x margin on the 1e-7 target (rimp2_gpu_gb300/tuning/split_buckets.json);
 // rimp2_set_split_buckets replaces it.
-static std::vector<std::pair<int, int>> g_buckets = {{0, 0},   {16, 2},  {128, 1},
+static std::vector<std::pair<int, int>> g_buckets = {{0, 0},   {16, 2},  {128, 2},
                                                      {192, 1}, {256, 1}, {384, 1}};
 static std::mutex g_bucket_mu;
 
