@@ -69,9 +69,10 @@ int rimp2_last_timing(float *ms4);
 /* Energy kernel of the last split-form launch: 0 none yet, 1 one-CTA tile
  * kernel (128x128 MMA), 2 paired-CTA kernel (cta_group::2, 256x128 MMA over
  * two occupied pairs, three products per element pair with a per-column
- * diagonal correction).  A one-residual-slice group uses the paired kernel
- * unless its dummy CTAs add more than 10% work; RIMP2_PAIR_KERNEL=0 or =1 in
- * the environment overrides that choice. */
+ * diagonal correction).  One-residual-slice fragments with nocc >= 10 and
+ * NBA >= 1024 use the paired kernel (shorter auxiliary spaces run faster on
+ * the one-CTA kernel); RIMP2_PAIR_KERNEL=0 or =1 in the environment
+ * overrides that choice. */
 int rimp2_last_split_kernel(void);
 /* Measured FP64 tensor-op (DMMA) throughput of this GPU in TFLOP/s, the
  * denominator for the plain kernel's roofline fraction. */

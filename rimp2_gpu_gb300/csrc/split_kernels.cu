@@ -1878,22 +1878,24 @@ struct Group {
   CUtensorMap tm;
   // paired-CTA kernel (one residual slice): its pair items and B-half map
   bool pair = false;
-  long long npitems = 0, pair_slots = 0;
+  long long npitems = 0;
   DevBuf pitems, dcorr;  // dcorr: per-column diagonal correction of the V product
   CUtensorMap tmB;
 };
 
-// A one-residual-slice group runs the paired-CTA kernel (three products per
-// element pair, 0.87x the one-CTA kernel's time on the nocc=128 nvirt=1024
-// NBA=4096 fragment) unless its dummy CTAs (an odd count of i <= j for some
-// j) add more than 10% to the work: at nocc = 8 they add 11%, at 16 5.9%.
-// RIMP2_PAIR_KERNEL=0 or =1 overrides the choice.
-bool pair_kernel_wanted(const Group &g) {
-  if (g.nsl != 2) return false;
+// Kernel choice per one-residual-slice fragment.  The paired-CTA kernel
+// (three products per element pair) runs in 0.87-0.95x the one-CTA kernel's
+// time once NBA >= 1024 (0.87x at nocc=128 nvirt=1024 NBA=4096), but its
+// per-item cost (the exchange-tile transpose, the cross-CTA hand-offs) loses
+// on short auxiliary spaces: 1.14-1.49x at NBA <= 512, even at 1024.  Its
+// dummy CTAs (an odd count of i <= j for some j) add 2 C(nocc) / (nocc
+// (nocc+1)/2) - 1 of work: over 10% below nocc = 10.  RIMP2_PAIR_KERNEL=0 or
+// =1 overrides the choice.
+bool pair_kernel_for(int nocc, int NBA) {
   const char *e = getenv("RIMP2_PAIR_KERNEL");
   if (e && e[0] == '0') return false;
   if (e && e[0] == '1') return true;
-  return (double)g.pair_slots <= 1.10 * (double)g.nitems;
+  return nocc >= 10 && NBA >= 1024;
 }
 
 int build_group(Group &g, cudaStream_t s) {
@@ -1916,7 +1918,6 @@ int build_group(Group &g, cudaStream_t s) {
     F.item_base = item;
     F.pitem_base = pitem;
     pitem += pair_items_before(F.nocc) * F.ntp;
-    g.pair_slots += 2 * pair_items_before(F.nocc) * F.ntp;
     const int np = F.nocc * (F.nocc + 1) / 2;
     eo += F.nocc;
     ev += F.nvpad;
@@ -1937,7 +1938,10 @@ int build_group(Group &g, cudaStream_t s) {
     set_error("split batch too large for one launch (rows=%lld, items=%lld)", g.R, g.nitems);
     return RIMP2_ERR_ARG;
   }
-  g.pair = pair_kernel_wanted(g) && g.npitems <= 2147483647LL;
+  if (g.pair && g.npitems > 2147483647LL) {
+    set_error("split batch too large for one launch (pair items=%lld)", g.npitems);
+    return RIMP2_ERR_ARG;
+  }
   const int planes = g.nsl + (g.pair ? 1 : 0);  // the paired kernel adds the V plane
   RIMP2_TRY(g.frags.alloc(sizeof(FragDesc) * g.nfrag, s));
   RIMP2_TRY(g.items.alloc(sizeof(int4) * (size_t)g.nitems, s));
@@ -2348,7 +2352,7 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
 // A planned batch: up to two slice-count groups, workspace and (optionally)
 // an instantiated CUDA graph of the whole evaluation.
 struct SplitPlan {
-  Group g[2];
+  Group g[3];  // one residual slice (one-CTA), two residual slices, one residual slice (paired)
   PlainPlan *plain = nullptr;  // fragments planned in plain FP64 (slice count 0)
   int nsm = 0;
   cudaGraphExec_t gexec = nullptr;
@@ -2386,6 +2390,8 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
   cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, dev);
   P->g[0].nsl = 2;
   P->g[1].nsl = 3;
+  P->g[2].nsl = 2;
+  P->g[2].pair = true;
   std::vector<PlainFrag> plain;
   for (int f = 0; f < nfrag; ++f) {
     if (nslices && nslices[f] == 0) {
@@ -2413,7 +2419,7 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
     F.Epair = Epair[f];
     F.Etot = Etot[f];
     const int ns = nslices ? nslices[f] : 1;
-    P->g[ns >= 2 ? 1 : 0].fh.push_back(F);
+    P->g[ns >= 2 ? 1 : (pair_kernel_for(F.nocc, F.NBA) ? 2 : 0)].fh.push_back(F);
   }
   for (auto &g : P->g) {
     if (g.fh.empty()) continue;
@@ -2473,7 +2479,7 @@ int split_plan_execute(SplitPlan *P, cudaStream_t s) {
   if (timed)
     for (int k = 0; k < 4; ++k) RIMP2_CK(cudaEventCreate(&ev[k]));
   // a plan of plain fragments only is timed as one kernel interval
-  const bool plain_only = !P->g[0].nfrag && !P->g[1].nfrag;
+  const bool plain_only = !P->g[0].nfrag && !P->g[1].nfrag && !P->g[2].nfrag;
   if (timed && plain_only) {
     RIMP2_CK(cudaEventRecord(ev[0], s));
     RIMP2_CK(cudaEventRecord(ev[1], s));
@@ -2519,7 +2525,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   const double *dCaC = dCa;
   RIMP2_TRY(split_plan_create(&P, 1, &a.nocc, &a.nvirt, &a.NBA, &dCaC, &a.eo, &a.ev, &a.Epair,
                               &a.Etot, &ns, false, s));
-  Group &g = P->g[ns >= 2 ? 1 : 0];
+  Group &g = P->g[0].nfrag ? P->g[0] : (P->g[1].nfrag ? P->g[1] : P->g[2]);
   const FragDesc &F = g.fh[0];
   const FragDesc *fr = g.frags.as<FragDesc>();
   int rc = RIMP2_OK;

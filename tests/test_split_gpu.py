@@ -194,11 +194,11 @@ def test_pair_kernel_batched(api, kernel_choice):
 
 
 def test_kernel_choice_is_reported(api, kernel_choice):
-    """One-residual-slice fragments run the paired kernel unless its dummy
-    CTAs would add more than 10% work (nocc = 6: 14%, nocc = 32: 3%); the
-    environment overrides the choice and the library says which kernel ran."""
+    """One-residual-slice fragments with nocc >= 10 and NBA >= 1024 run the
+    paired kernel, the rest the one-CTA kernel; the environment overrides the
+    choice and the library says which kernel ran."""
     small = O.gen_fragment(31, 6, 200, 256)
-    big = O.gen_fragment(32, 32, 130, 128)
+    big = O.gen_fragment(32, 32, 130, 1024)
     kernel_choice("")
     dev_energy(api, *small, 1)
     assert api.last_split_kernel() == 1
