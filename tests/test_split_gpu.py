@@ -214,7 +214,7 @@ def test_kernel_choice_is_reported(api, kernel_choice):
     assert api.last_split_kernel() == 1
 
 
-@pytest.mark.parametrize("nocc,nvirt,NBA", [(33, 256, 1000), (9, 130, 512)])
+@pytest.mark.parametrize("nocc,nvirt,NBA", [(33, 256, 1000), (9, 200, 512)])
 def test_pair_kernel_host_streamed(api, kernel_choice, nocc, nvirt, NBA):
     """The host-pointer split call copies Calpha in occupied chunks and runs
     the paired kernel on each chunk's pair items as the chunk lands."""
