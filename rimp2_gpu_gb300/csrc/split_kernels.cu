@@ -31,6 +31,11 @@
 //   memory.  T1 is read out and released first, so the next item's T1 MMAs
 //   overlap this item's T2 phase; diagonal tile pairs take T2 = T1^T through
 //   shared memory.
+// A one-residual-slice fragment with nocc >= 10 and NBA >= 1024 runs instead
+// on split_pair_kernel: clusters of two CTAs issuing cta_group::2 MMAs over
+// two occupied pairs that share their B operand, with a third slice plane
+// V = fp16(C*s) that folds R1a S0b + R1a R1b into R1a V (three products per
+// element pair, a per-column correction removing the same-column bias).
 // Every wait on an mbarrier is bounded by a clock budget; on expiry the
 // kernel records an error code, drains its own copies and MMAs, frees TMEM
 // and returns, and the host reports RIMP2_ERR_TIMEOUT.
@@ -1144,7 +1149,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
               const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
               // [L0 | L1] += S0a x [S0b; R1b]: exact integer part and S0a R1b
               mma_f16_pair(dL0, a0, by, IDESC_PAIR_N256, acc);
-              mma_f16_pair(dL1, a1, bw, IDESC_PAIR, 1u);  // R1a V = R1a (S0b + R1b) + ...
+              mma_f16_pair(dL1, a1, bw, IDESC_PAIR, 1u);  // R1a V (= R1a S0b + R1a R1b + R1a eps)
             }
             mma_commit_pair(empty0 + 8 * stage);  // frees the stage in both CTAs
             if (++stage == NSTAGE) {
