@@ -1405,7 +1405,15 @@ struct EosParams {
   int *err;
   int nocc, nvirt, nvpad, nks, ntp, ncol;
   int rowC, rowCt;           // first slice row of C and of Ct (per plane)
+  const float *dcorr;        // one residual slice: per column sum_k R1 (V - S0 - R1)
 };
+
+// One residual slice adds the V plane (three products per element pair, as
+// in split_pair_kernel): a stage holds S0a, R1a (128 rows) and S0b, R1b, Vb
+// (64 rows).
+constexpr int eos_stage_bytes(int nsl) {
+  return nsl * PANEL_BYTES + (nsl + (nsl == 2 ? 1 : 0)) * HPANEL_BYTES;
+}
 
 __device__ __forceinline__ void eos_decode(const EosParams &P, long long id, int &i, int &j,
                                            int &tA, int &tB, int &h) {
@@ -1422,7 +1430,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                      EosParams P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  constexpr int STAGE_BYTES = NSL * (PANEL_BYTES + HPANEL_BYTES);
+  constexpr bool VP = (NSL == 2);  // V plane: R1a S0b + R1a R1b folded into R1a V
+  constexpr int STAGE_BYTES = eos_stage_bytes(NSL);
   constexpr int NEPI = 8;
   uint8_t *stages = base;
   uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
@@ -1521,6 +1530,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               tma_load_3d(dst + NSL * PANEL_BYTES + sl * HPANEL_BYTES, &tmB, fb, 0, rowk + colB,
                           sl);
             }
+            if (VP)
+              tma_load_3d(dst + NSL * PANEL_BYTES + NSL * HPANEL_BYTES, &tmB, fb, 0, rowk + colB,
+                          NSL);  // V
             if (++stage == NSTAGE) {
               stage = 0;
               phase ^= 1;
@@ -1589,6 +1601,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
               // [L0 | L1] += S0a x [S0b; R1b]: exact integer part and S0a R1b
               mma_f16_id(dL0, a0, b0, idesc2, acc);
+              if (VP) {  // R1a V (= R1a S0b + R1a R1b + R1a eps)
+                mma_f16_id(dL1, a1, smem_desc(sbB + NSL * HPANEL_BYTES + koff), idesc, 1u);
+                continue;
+              }
               mma_f16_id(dL1, a1, b0, idesc, 1u);   // R1a S0b
               mma_f16_id(dL1, a1, b1, idesc, 1u);   // R1a R1b
               if (NSL > 2) {
@@ -1682,6 +1698,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         ok = false;
         break;
       }
+      if (VP && same && diag) {
+        // g_ii(a,a) and gt_ii(a,a): remove the same-column bias of R1a V
+        const int cd = a - b0;  // this row's diagonal element among the thread's 32 columns
+        if (cd >= 0 && cd < 32) {
+          const float cg = P.dcorr[i * P.nvpad + a] * (sCi * sCi);
+          const float cu = P.dcorr[P.ncol + i * P.nvpad + a] * (sTi * sTi);
+#pragma unroll
+          for (int k = 0; k < 32; ++k)
+            if (k == cd) {
+              g1[k] -= cg;
+              u1[k] -= cu;
+            }
+        }
+      }
       double eacc = 0.0;
       if (same) {
         float ef = 0.0f;
@@ -1740,7 +1770,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }
 
 int eos_smem_bytes(int nsl, int nstage) {
-  return nstage * nsl * (PANEL_BYTES + HPANEL_BYTES) + 1024 + 512;
+  return nstage * eos_stage_bytes(nsl) + 1024 + 512;
 }
 
 // Self-test of the bounded-wait path: one thread waits on an mbarrier that
@@ -2819,10 +2849,13 @@ int split_eos_energy(const double *Ca, const double *Ct, int NBA, int nvirt, int
     F.eo = eo;
     F.ev = ev;
   }
-  DevBuf frags, slices, inv, eo2, ev2, part, queue, pairs;
+  const int vplane = nsl == 2 ? 1 : 0;  // one residual slice: V plane, three products
+  const int planes = nsl + vplane;
+  DevBuf frags, slices, inv, eo2, ev2, part, queue, pairs, dcorr;
   RIMP2_TRY(frags.alloc(sizeof fh, s));
-  RIMP2_TRY(slices.alloc(sizeof(__half) * (size_t)nsl * R * 64, s));
+  RIMP2_TRY(slices.alloc(sizeof(__half) * (size_t)planes * R * 64, s));
   RIMP2_TRY(inv.alloc(sizeof(float) * 2 * (size_t)ncol, s));
+  if (vplane) RIMP2_TRY(dcorr.alloc(sizeof(float) * 2 * (size_t)ncol, s));
   RIMP2_TRY(eo2.alloc(sizeof(float2) * nocc, s));
   RIMP2_TRY(ev2.alloc(sizeof(float2) * nvpad, s));
   RIMP2_TRY(part.alloc(sizeof(double) * (size_t)nitems, s));
@@ -2831,12 +2864,13 @@ int split_eos_energy(const double *Ca, const double *Ct, int NBA, int nvirt, int
   RIMP2_CK(cudaMemcpyAsync(frags.p, fh, sizeof fh, cudaMemcpyHostToDevice, s));
   const FragDesc *fr = frags.as<FragDesc>();
   slice_batch_kernel<<<dim3((unsigned)((ncol * 32 + 255) / 256), 2), 256, 0, s>>>(
-      fr, nsl, R * 64, slices.as<__half>(), inv.as<float>(), 0, 0x7fffffff);
+      fr, nsl, R * 64, slices.as<__half>(), inv.as<float>(), 0, 0x7fffffff, vplane,
+      dcorr.as<float>());
   eps_batch_kernel<<<dim3((unsigned)((std::max(nvpad, nocc) + 255) / 256), 1), 256, 0, s>>>(
       fr, eo2.as<float2>(), ev2.as<float2>());
   count_launch(2);
   CUtensorMap tmA, tmB;
-  cuuint64_t dims[3] = {64, (cuuint64_t)R, (cuuint64_t)nsl};
+  cuuint64_t dims[3] = {64, (cuuint64_t)R, (cuuint64_t)planes};
   cuuint64_t strides[2] = {128, (cuuint64_t)R * 128};
   cuuint32_t boxA[3] = {KSTEP, TILE, 1}, boxB[3] = {KSTEP, HALF, 1};
   cuuint32_t estr[3] = {1, 1, 1};
@@ -2867,6 +2901,7 @@ int split_eos_energy(const double *Ca, const double *Ct, int NBA, int nvirt, int
   P.ncol = (int)ncol;
   P.rowC = 0;
   P.rowCt = (int)((long long)nks * ncol);
+  P.dcorr = dcorr.as<float>();
   int dev = 0, nsm = 0;
   RIMP2_CK(cudaGetDevice(&dev));
   RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
