@@ -1674,6 +1674,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float bw = dh0 - sh;
       const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
       // one tile's 32 columns of this thread into registers, then release it
+      // g_ii(a,a) and gt_ii(a,a) of the one-residual (V plane) form carry the
+      // same-column bias sum_k R1 (V - S0 - R1): its column among the
+      // thread's 32 (or -1) and the two corrections, removed as T1/U1 are read
+      const int cd = (VP && same && diag && a - b0 >= 0 && a - b0 < 32) ? a - b0 : -1;
+      const float cg = cd >= 0 ? P.dcorr[i * P.nvpad + a] : 0.0f;
+      const float cu = cd >= 0 ? P.dcorr[P.ncol + i * P.nvpad + a] : 0.0f;
       auto take = [&](int t, const float *sr, float srow, float (&v)[32]) -> bool {
         const bool w = mbar_wait(tfull0 + 8 * t, (par >> t) & 1, abort_flag, P.err, 4);
         if (epi_any(!w)) return false;
@@ -1685,7 +1691,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           tmem_ld16(tbase + t * 2 * HALF + HALF + c0, l1);
           tmem_wait_ld();
 #pragma unroll
-          for (int k = 0; k < 16; ++k) v[c0 + k] = (l0[k] + l1[k]) * (srow * sr[b0 + c0 + k]);
+          for (int k = 0; k < 16; ++k) {
+            float x = l0[k] + l1[k];
+            if (t == 0 && c0 + k == cd) x -= cg;
+            if (t == 2 && c0 + k == cd) x -= cu;
+            v[c0 + k] = x * (srow * sr[b0 + c0 + k]);
+          }
         }
         tc_fence_before();
         __syncwarp();
@@ -1698,20 +1709,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         ok = false;
         break;
       }
-      if (VP && same && diag) {
-        // g_ii(a,a) and gt_ii(a,a): remove the same-column bias of R1a V
-        const int cd = a - b0;  // this row's diagonal element among the thread's 32 columns
-        if (cd >= 0 && cd < 32) {
-          const float cg = P.dcorr[i * P.nvpad + a] * (sCi * sCi);
-          const float cu = P.dcorr[P.ncol + i * P.nvpad + a] * (sTi * sTi);
-#pragma unroll
-          for (int k = 0; k < 32; ++k)
-            if (k == cd) {
-              g1[k] -= cg;
-              u1[k] -= cu;
-            }
-        }
-      }
+
       double eacc = 0.0;
       if (same) {
         float ef = 0.0f;
