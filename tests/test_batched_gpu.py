@@ -90,3 +90,35 @@ def test_bucket_table_roundtrip():
     assert t["buckets"][0]["nvirt_min"] == 0
     for b in t["buckets"]:
         assert api.split_nslices(max(b["nvirt_min"], 1), 4, 64) == b["nslices"]
+
+
+def test_batch_plan_all_four_groups():
+    """One plan with a fragment in each launch group: paired-CTA kernel
+    (one residual slice, nocc >= 10, NBA >= 1024), one-CTA kernel with one
+    and with two residual slices, and plain FP64 -- one persistent launch
+    sequence per group, every fragment against the oracle."""
+    import torch
+    from rimp2_gpu_gb300 import api
+    shapes = [(12, 256, 1024, 1), (11, 200, 300, 1), (5, 130, 777, 2), (8, 64, 256, 0)]
+    dev, ref = [], []
+    for k, (nocc, nvirt, NBA, _) in enumerate(shapes):
+        Ca, eo, ev = O.gen_fragment(800 + k, nocc, nvirt, NBA)
+        ref.append(O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True))
+        dev.append(dict(C=torch.from_numpy(Ca.ravel(order="F")).cuda(),
+                        eo=torch.from_numpy(eo).cuda(), ev=torch.from_numpy(ev).cuda(),
+                        E=torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda"),
+                        T=torch.zeros(1, dtype=torch.float64, device="cuda")))
+    desc = [(n, v, b, t["C"].data_ptr(), t["eo"].data_ptr(), t["ev"].data_ptr(), t["E"].data_ptr(),
+             t["T"].data_ptr()) for (n, v, b, _), t in zip(shapes, dev)]
+    plan = api.BatchPlan(desc, nslices=[s[3] for s in shapes], graph=True)
+    n0 = api.kernel_launch_count()
+    plan.execute()
+    torch.cuda.synchronize()
+    api.sync_status()
+    assert api.kernel_launch_count() - n0 == 3 + 5 + 5 + 5
+    plan.close()
+    for (n, _, _, ns), t, (Epr, Er) in zip(shapes, dev, ref):
+        tol = 1e-11 if ns == 0 else 1e-7
+        Ep = t["E"].cpu().numpy().reshape(n, n, order="F")
+        assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= tol
+        assert abs(t["T"].item() - Er) <= tol * abs(Er)
