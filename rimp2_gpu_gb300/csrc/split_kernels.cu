@@ -731,6 +731,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const bool w2 = mbar_wait(t2full, (uint32_t)(nloc & 1), abort_flag, P.err, 8);
       if (epi_any(!w2)) break;
       tc_fence_after();
+      // items that do not read T2 (i = j, or A = B with T2 = T1^T) hand it
+      // back to the MMA issuer at once
+      bool t2_held = true;
+      if (same || diag) {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(t2empty);
+        t2_held = false;
+      }
       const uint32_t t2 = tmem + lane_off + 2 * TILE + cbase;
       // one 16-column chunk of energy terms, g2 supplied by `g2at(k)`
       auto terms = [&](int c0, const float *g2) -> float {
@@ -790,9 +799,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           eacc += (double)terms(c0, g2);
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(t2empty);
+      if (t2_held) {
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(t2empty);
+      }
       // reduce the item's energy over the epilogue threads
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
@@ -1252,6 +1263,19 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
       const bool w2 = pair_wait(t2full, (uint32_t)(nloc & 1), false, abort_flag, abort_peer, P.err, 8);
       if (epi_any(!w2)) break;
       tc_fence_after();
+      // each warp hands T2' back to the MMA issuer as soon as it has read its
+      // rows (or at once when this item does not read T2'), so that the next
+      // item's second chain can start while the energy terms are formed
+      bool t2_held = true;
+      auto release_t2 = [&]() {
+        if (t2_held) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive_remote(t2empty_L);
+          t2_held = false;
+        }
+      };
+      if (dummy || same || diag) release_t2();
       double eacc = 0.0;
       if (!dummy) {
         if (same) {  // g_ii is symmetric
@@ -1287,6 +1311,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
 #pragma unroll
                   for (int k = 0; k < 16; ++k) dst[c0 + k] = (l0[k] + l1[k]) * (sbi * saj[c0 + k]);
                 }
+                release_t2();
               }
             }
             asm volatile("bar.sync 1, 256;" ::: "memory");
@@ -1302,9 +1327,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
           }
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive_remote(t2empty_L);
+      release_t2();
       // reduce the item's energy over the epilogue threads
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
