@@ -254,9 +254,11 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
                          const int *precision);
 
 /* Batched energies of many fragments of uneven size, all resident on the
- * device, in ONE persistent launch per slice-count group: a device-side
- * queue of (fragment, pair i<=j, tile pair) work items ordered heaviest
- * fragment first, drained by one CTA per SM.  nslices[f] = 1 or 2 runs
+ * device, in ONE persistent launch per kernel group (one residual slice on
+ * the paired-CTA kernel -- nocc >= 10 and NBA >= 1024 -- or on the one-CTA
+ * kernel, two residual slices, plain FP64): a device-side queue of
+ * (fragment, pair, tile pair) work items ordered heaviest fragment first,
+ * drained by one CTA (pair of CTAs) per SM (pair of SMs).  nslices[f] = 1 or 2 runs
  * fragment f in the split form with that many residual slices; 0 runs it in
  * plain FP64 (the fused DMMA kernel's tile pairs, drained by one persistent
  * launch over all FP64 fragments of the plan).  With use_graph != 0 the

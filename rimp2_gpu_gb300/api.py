@@ -285,7 +285,8 @@ def gen_fragment_dev(seed, nocc, nvirt, NBA, dCalpha=0, dEVocc=0, dEVvirt=0, str
 
 class BatchPlan:
     """Batched energies of many device-resident fragments: one persistent
-    launch per slice-count group draining a device work queue, optionally
+    launch per group (paired-CTA kernel, one-CTA kernel with one or two
+    residual slices, plain FP64) draining a device work queue, optionally
     captured once as a CUDA graph (C-ABI rimp2_batch_plan_*).  ``frags`` is
     a list of (nocc, nvirt, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot)
     with device addresses; ``nslices`` per fragment is 1 or 2 (split form)

@@ -1139,7 +1139,7 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
   RIMP2_TRY(ensure_device());
   cudaStream_t s = current_stream();
   // one device copy of every fragment (inputs are in HBM together; the
-  // split form then runs the whole batch as one persistent launch)
+  // split form then runs the batch as one persistent launch per kernel group)
   size_t nca = 0, neo = 0, nev = 0, nep = 0;
   for (int f = 0; f < nf; ++f) {
     nca += (size_t)NBA[f] * nvirt[f] * nocc[f];

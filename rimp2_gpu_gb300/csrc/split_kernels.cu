@@ -1922,8 +1922,9 @@ int smem_bytes(int nsl, int nstage) {
          64 * TP * 4 /*diagonal-tile transpose buffer*/;
 }
 
-// One slice-count group of a batch: its fragments share a slice count, a
-// slices buffer, one tensor map and one persistent launch.
+// One launch group of a batch: its fragments share a slice count and an
+// energy kernel (one-CTA or paired), a slices buffer, the tensor maps and one
+// persistent launch.
 struct Group {
   int nsl = 2;
   int nfrag = 0;
@@ -2405,7 +2406,7 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
 
 }  // namespace
 
-// A planned batch: up to two slice-count groups, workspace and (optionally)
+// A planned batch: up to three launch groups, workspace and (optionally)
 // an instantiated CUDA graph of the whole evaluation.
 struct SplitPlan {
   Group g[3];  // one residual slice (one-CTA), two residual slices, one residual slice (paired)
