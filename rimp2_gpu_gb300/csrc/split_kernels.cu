@@ -67,6 +67,13 @@ constexpr int KSTEP = 64;      // K per stage (one 128-byte swizzle row of FP16)
 constexpr int PANEL_BYTES = TILE * KSTEP * 2;  // 16 KB
 constexpr int NTHREADS = 320;  // producer warp, MMA warp, 8 epilogue warps
 constexpr long long WAIT_BUDGET = 4000000000LL;  // ~2 s of SM clock per wait
+// split_batch_kernel: producer warp, MMA warp and 16 epilogue warps (four per
+// TMEM lane quadrant, 32 accumulator columns each).  On short auxiliary
+// spaces the epilogue, not the MMAs, bounds a work item; eight warps left two
+// per scheduler to hide the TMEM-load, MUFU and FMA latencies.
+constexpr int BATCH_EPI = 16;
+constexpr int BATCH_THREADS = 64 + 32 * BATCH_EPI;
+constexpr int BATCH_REGS = 65536 / BATCH_THREADS / 8 * 8;  // 112: the whole register file
 
 // --------------------------------------------------------------------------
 // small PTX helpers
@@ -126,6 +133,20 @@ __device__ __forceinline__ bool epi_any(bool p) {
       "{\n\t.reg .pred q, o;\n\t"
       "setp.ne.u32 q, %1, 0;\n\t"
       "bar.red.or.pred o, 1, 256, q;\n\t"
+      "selp.u32 %0, 1, 0, o;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p)
+      : "memory");
+  return r != 0;
+}
+
+// the same over the 512 epilogue threads of split_batch_kernel
+__device__ __forceinline__ bool epi_any512(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, o;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred o, 1, 512, q;\n\t"
       "selp.u32 %0, 1, 0, o;\n\t}"
       : "=r"(r)
       : "r"((uint32_t)p)
@@ -473,12 +494,12 @@ constexpr int IQ = 4;  // item ring depth between the producer and the consumers
 constexpr int TP = TILE + 1;  // padded row of the diagonal-tile transpose buffer (floats)
 
 template <int NSL, int NSTAGE>
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __maxnreg__(BATCH_REGS)
     split_batch_kernel(const __grid_constant__ CUtensorMap tmap, BatchParams P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int STAGE_BYTES = NSL * 2 * PANEL_BYTES;
-  constexpr int NEPI = 8;  // epilogue warps: two per TMEM lane quadrant
+  constexpr int NEPI = BATCH_EPI;  // epilogue warps: four per TMEM lane quadrant
   uint8_t *stages = base;
   uint64_t *bars = (uint64_t *)(base + NSTAGE * STAGE_BYTES);
   // bars: full[NSTAGE], empty[NSTAGE], t1full, t1empty, t2full, t2empty, drain,
@@ -667,9 +688,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else {
     // ------------------------------ epilogue ----------------------------------
-    const int ew = warp - 2;             // 0..7
+    const int ew = warp - 2;             // 0..15
     const int quad = warp & 3;           // TMEM lane quadrant this warp may access
-    const int cbase = (ew >> 2) * 64;    // column half of the tile this warp reads
+    const int cbase = (ew >> 2) * 32;    // the 32 columns of the tile this warp reads
     const int row = quad * 32 + lane;    // tile row = a offset
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     int islot = 0;
@@ -677,7 +698,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     long long nloc = 0;
     while (true) {
       const bool w0 = mbar_wait(ifull0 + 8 * islot, iphase, abort_flag, P.err, 7);
-      if (epi_any(!w0)) break;
+      if (epi_any512(!w0)) break;
       const int qidx = item_q[islot];
       __syncwarp();
       if (lane == 0) mbar_arrive(iempty0 + 8 * islot);
@@ -700,12 +721,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float2 *evb = P.ev2 + F.ev_off + tB * TILE + cbase;
       // ---- T1 -> registers, then hand its TMEM back to the MMA issuer ----
       const bool w1 = mbar_wait(t1full, (uint32_t)(nloc & 1), abort_flag, P.err, 4);
-      if (epi_any(!w1)) break;
+      if (epi_any512(!w1)) break;
       tc_fence_after();
       const uint32_t t1 = tmem + lane_off + cbase;
-      float g1[64];
+      float g1[32];
 #pragma unroll
-      for (int c0 = 0; c0 < 64; c0 += 16) {
+      for (int c0 = 0; c0 < 32; c0 += 16) {
         float l0[16], l1[16];
         tmem_ld16(t1 + c0, l0);
         tmem_ld16(t1 + TILE + c0, l1);
@@ -729,7 +750,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float dl0 = ((sh - (dh0 - bw)) + (-ea.x - bw)) + (sl - ea.y);
       // ---- T2 and the energy terms ----
       const bool w2 = mbar_wait(t2full, (uint32_t)(nloc & 1), abort_flag, P.err, 8);
-      if (epi_any(!w2)) break;
+      if (epi_any512(!w2)) break;
       tc_fence_after();
       // items that do not read T2 (i = j, or A = B with T2 = T1^T) hand it
       // back to the MMA issuer at once
@@ -764,26 +785,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         // two 64-row passes; pass h serves the warps that own columns [64h,64h+64)
 #pragma unroll 1
         for (int h = 0; h < 2; ++h) {
-          asm volatile("bar.sync 1, 256;" ::: "memory");
+          asm volatile("bar.sync 1, 512;" ::: "memory");
           if ((row >> 6) == h) {
             float *dst = tbuf + (row - 64 * h) * TP + cbase;
 #pragma unroll
-            for (int k = 0; k < 64; ++k) dst[k] = g1[k];
+            for (int k = 0; k < 32; ++k) dst[k] = g1[k];
           }
-          asm volatile("bar.sync 1, 256;" ::: "memory");
+          asm volatile("bar.sync 1, 512;" ::: "memory");
           if ((cbase >> 6) == h) {
 #pragma unroll
-            for (int c0 = 0; c0 < 64; c0 += 16) {
+            for (int c0 = 0; c0 < 32; c0 += 16) {
               float g2[16];
 #pragma unroll
-              for (int k = 0; k < 16; ++k) g2[k] = tbuf[(c0 + k) * TP + row];
+              for (int k = 0; k < 16; ++k) g2[k] = tbuf[(cbase - 64 * h + c0 + k) * TP + row];
               eacc += (double)terms(c0, g2);
             }
           }
         }
       } else {
 #pragma unroll
-        for (int c0 = 0; c0 < 64; c0 += 16) {
+        for (int c0 = 0; c0 < 32; c0 += 16) {
           float g2[16];
           if (same) {
 #pragma unroll
@@ -808,14 +829,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
       if (lane == 0) redd[ew] = eacc;
-      asm volatile("bar.sync 1, 256;" ::: "memory");
+      asm volatile("bar.sync 1, 512;" ::: "memory");
       if (ew == 0 && lane == 0) {
         double tot = 0.0;
 #pragma unroll
         for (int w = 0; w < NEPI; ++w) tot += redd[w];
         P.part[it.w] = tot;
       }
-      asm volatile("bar.sync 1, 256;" ::: "memory");
+      asm volatile("bar.sync 1, 512;" ::: "memory");
       ++nloc;
     }
   }
@@ -2105,10 +2126,10 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
     note_split_kernel(2);
   } else if (g.nsl == 2) {
     note_split_kernel(1);
-    split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, P);
+    split_batch_kernel<2, 3><<<grid, BATCH_THREADS, smem_bytes(2, 3), s>>>(g.tm, P);
   } else {
     note_split_kernel(1);
-    split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, P);
+    split_batch_kernel<3, 2><<<grid, BATCH_THREADS, smem_bytes(3, 2), s>>>(g.tm, P);
   }
   count_launch(1);
   if (ev) RIMP2_CK(cudaEventRecord(ev[2], s));
@@ -2662,9 +2683,9 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
       const int grid = (int)std::min<long long>(BP.nitems - BP.item_begin, P->nsm);
       note_split_kernel(1);
       if (g.nsl == 2)
-        split_batch_kernel<2, 3><<<grid, NTHREADS, smem_bytes(2, 3), s>>>(g.tm, BP);
+        split_batch_kernel<2, 3><<<grid, BATCH_THREADS, smem_bytes(2, 3), s>>>(g.tm, BP);
       else
-        split_batch_kernel<3, 2><<<grid, NTHREADS, smem_bytes(3, 2), s>>>(g.tm, BP);
+        split_batch_kernel<3, 2><<<grid, BATCH_THREADS, smem_bytes(3, 2), s>>>(g.tm, BP);
     }
     count_launch(2);
     e = cudaGetLastError();
