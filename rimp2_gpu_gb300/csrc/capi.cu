@@ -1184,7 +1184,7 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
                                       *precision == RIMP2_PREC_SPLIT ? nullptr : zeros.data(), 0,
                                       s));
     int rc = rimp2_batch_plan_execute(plan, s);
-    rimp2_batch_plan_destroy(plan);
+    split_plan_destroy((SplitPlan *)plan);  // keeps the error message of a failed execute
     RIMP2_TRY(rc);
   }
   oe = 0;

@@ -73,7 +73,6 @@ constexpr long long WAIT_BUDGET = 4000000000LL;  // ~2 s of SM clock per wait
 // per scheduler to hide the TMEM-load, MUFU and FMA latencies.
 constexpr int BATCH_EPI = 16;
 constexpr int BATCH_THREADS = 64 + 32 * BATCH_EPI;
-constexpr int BATCH_REGS = 65536 / BATCH_THREADS / 8 * 8;  // 112: the whole register file
 
 // --------------------------------------------------------------------------
 // small PTX helpers
@@ -494,7 +493,7 @@ constexpr int IQ = 4;  // item ring depth between the producer and the consumers
 constexpr int TP = TILE + 1;  // padded row of the diagonal-tile transpose buffer (floats)
 
 template <int NSL, int NSTAGE>
-__global__ void __maxnreg__(BATCH_REGS)
+__global__ void __launch_bounds__(BATCH_THREADS, 1)
     split_batch_kernel(const __grid_constant__ CUtensorMap tmap, BatchParams P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
