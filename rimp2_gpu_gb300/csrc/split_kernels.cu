@@ -17,12 +17,12 @@
 //   FP64 across threads; pair and total energies are reduced in FP64 with
 //   compensation.
 //
-// Kernel layout (one persistent CTA per SM, 320 threads):
-//   warp 0      TMA producer (128x64 FP16 boxes, 128B swizzle) and the
-//               device-side work queue (atomic counter, 4-deep item ring)
-//   warp 1      TMEM owner + single-thread tcgen05.mma issuer
-//   warps 2..9  epilogue, two warps per TMEM lane quadrant: tcgen05.ld of the
-//               accumulators, denominators, energy terms
+// Kernel layout (one persistent CTA per SM, 576 threads):
+//   warp 0       TMA producer (128x64 FP16 boxes, 128B swizzle) and the
+//                device-side work queue (atomic counter, 4-deep item ring)
+//   warp 1       TMEM owner + single-thread tcgen05.mma issuer
+//   warps 2..17  epilogue, four warps per TMEM lane quadrant (32 accumulator
+//                columns each): tcgen05.ld, denominators, energy terms
 //   Work item = (fragment, pair i<=j, tile pair A<=B): T1 = G_ij[A,B] =
 //   C_iA^T C_jB and T2 = G_ji[A,B] = C_jA^T C_iB, each with L0/L1
 //   accumulators in TMEM (4 x 128 columns = all 512).  The exchange integral
@@ -68,9 +68,11 @@ constexpr int PANEL_BYTES = TILE * KSTEP * 2;  // 16 KB
 constexpr int NTHREADS = 320;  // producer warp, MMA warp, 8 epilogue warps
 constexpr long long WAIT_BUDGET = 4000000000LL;  // ~2 s of SM clock per wait
 // split_batch_kernel: producer warp, MMA warp and 16 epilogue warps (four per
-// TMEM lane quadrant, 32 accumulator columns each).  On short auxiliary
-// spaces the epilogue, not the MMAs, bounds a work item; eight warps left two
-// per scheduler to hide the TMEM-load, MUFU and FMA latencies.
+// TMEM lane quadrant, 32 accumulator columns each; the launch bounds give
+// them 96 registers).  On short auxiliary spaces a work item is bounded by
+// its epilogue and hand-offs, not by its MMAs; 16 warps instead of 8 took
+// 5-7% off such items (nocc=64 nvirt=512 NBA=256) and left long ones as
+// they were.
 constexpr int BATCH_EPI = 16;
 constexpr int BATCH_THREADS = 64 + 32 * BATCH_EPI;
 
