@@ -184,3 +184,9 @@ def test_datafile_rejects_bad_files(tmp_path):
     assert ei.value.status == 1
     with pytest.raises(_lib.Rimp2Error):
         api.read_datafile(str(tmp_path / "missing.data"))
+
+
+def test_split_kernel_report_before_any_launch():
+    """The kernel-choice report is a host-side read: 0 before any split launch."""
+    from rimp2_gpu_gb300 import api
+    assert api.last_split_kernel() == 0
