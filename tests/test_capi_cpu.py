@@ -187,6 +187,12 @@ def test_datafile_rejects_bad_files(tmp_path):
 
 
 def test_split_kernel_report_before_any_launch():
-    """The kernel-choice report is a host-side read: 0 before any split launch."""
-    from rimp2_gpu_gb300 import api
-    assert api.last_split_kernel() == 0
+    """The kernel-choice report is a host-side read: 0 in a fresh process
+    before any split launch."""
+    import subprocess
+    import sys
+    out = subprocess.run([sys.executable, "-c", "from rimp2_gpu_gb300 import api; "
+                          "print(api.last_split_kernel())"], cwd=ROOT, capture_output=True,
+                         text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == "0"
