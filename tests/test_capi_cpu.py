@@ -196,3 +196,29 @@ def test_split_kernel_report_before_any_launch():
                          text=True, timeout=120)
     assert out.returncode == 0, out.stderr
     assert out.stdout.strip() == "0"
+
+
+def test_fortran_module_matches_header():
+    """Every bind(C) interface of the Fortran module names a function that
+    include/rimp2_gpu.h declares and the library exports, with the same
+    number of arguments (the module cannot be compiled here: no Fortran
+    compiler in this run)."""
+    import ctypes
+    import re
+    hdr = open(os.path.join(ROOT, "include", "rimp2_gpu.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(?:int|long long|const char\s*\*)\s*(rimp2_\w+)\s*\(([^)]*)\)\s*;", hdr):
+        args = m.group(2).strip()
+        protos[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    f90 = open(os.path.join(ROOT, "rimp2_gpu_gb300", "fortran", "rimp2_gpu_interfaces.F90")).read()
+    f90 = re.sub(r"&\s*\n\s*&?", " ", f90)  # join continuation lines
+    found = re.findall(r"function\s+(\w+)\s*\(([^)]*)\)\s*bind\s*\(\s*C\s*,\s*name\s*=\s*\"(\w+)\"",
+                       f90, flags=re.I)
+    assert len(found) == f90.count("bind(C, name=")
+    lib = ctypes.CDLL(os.path.join(ROOT, "rimp2_gpu_gb300", "librimp2_gpu_gb300.so"))
+    for fname, args, cname in found:
+        assert cname in protos, f"{cname} is not declared in rimp2_gpu.h"
+        nargs = 0 if not args.strip() else args.count(",") + 1
+        assert nargs == protos[cname], f"{cname}: {nargs} Fortran arguments, {protos[cname]} in C"
+        assert hasattr(lib, cname), f"{cname} is not exported"
