@@ -206,7 +206,11 @@ int rimp2_datafile_write(const char *path, const int *hdr, int first_order,
  * RIMP2_calc_toccA, RIMP2.F90:397-404) --------------------------------------
  * e_ij = sum_ab t_ij^ab (2 g_ij^ab - g_ij^ba),  t = g / (e_i+e_j-e_a-e_b),
  * Epair(nocc,nocc) symmetric, Etot = sum_ij e_ij.
- * precision: RIMP2_PREC_FP64 or RIMP2_PREC_SPLIT.  tamp (optional, may be
+ * precision: RIMP2_PREC_FP64 (FP64 DMMA, 1e-11 of the FP64 oracle) or
+ * RIMP2_PREC_SPLIT (FP16 Ozaki slices on tcgen05: every pair energy and the
+ * total within 1e-7 relative of FP64; the integer part of each product is
+ * accumulated exactly, the corrections in FP32, the epilogue in FP32 with
+ * double-float denominators and FP64 reductions).  tamp (optional, may be
  * NULL, FP64 path only) receives t(a,i,b,j) in layout (nvirt,nocc,nvirt,nocc). */
 int rimp2_energy(const int *nvirt, const int *nocc, const int *NBA, const double *Calpha,
                  const double *EVocc, const double *EVvirt, double *Epair, double *Etot,
