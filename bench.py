@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="CPU-baseline sample length; 0 skips it")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e leg")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the compact batched (config 4) and AO pipeline (config 5) legs "
+                         "of the default run")
     ap.add_argument("--workload", choices=["fragment", "batched", "ao", "eos"],
                     default="fragment",
                     help="fragment: one nocc=128/nvirt=1024/NBA=4096 fragment (default); "
@@ -222,7 +225,11 @@ def allmax(pg, v):
 
 
 OCC_SAMPLE = [0, 1, 63, 64, 126, 127]
-PAIR_SAMPLE = [(0, 1), (63, 64), (126, 127), (0, 127), (1, 63), (64, 126), (0, 0), (127, 127)]
+# every pair i <= j of the sampled occupied indices (21), interleaved so that a
+# short sample still mixes near-diagonal, far and i = j pairs
+PAIR_SAMPLE = [(0, 1), (63, 64), (126, 127), (0, 127), (1, 63), (64, 126), (0, 0), (127, 127),
+               (0, 63), (1, 126), (63, 127), (0, 64), (1, 127), (64, 64), (63, 126), (0, 126),
+               (1, 1), (64, 127), (1, 64), (63, 63), (126, 126)]
 
 
 def sample_inputs(Ca_host=None, eo=None, ev=None):
@@ -248,9 +255,12 @@ def cpu_reference_sample(seconds, sub, eo_s, ev, pairs_per_step=None, start=0):
     idx = {o: k for k, o in enumerate(OCC_SAMPLE)}
     done, flop, t0 = 0, 0.0, time.perf_counter()
     used_pairs = []
+    energies = {}
     while True:
         i, j = pairs_all[(start + done) % len(pairs_all)]
-        O.pair_energies(NVIRT, len(OCC_SAMPLE), NBA, sub, eo_s, ev, pairs=[(idx[i], idx[j])])
+        Ep_s, _ = O.pair_energies(NVIRT, len(OCC_SAMPLE), NBA, sub, eo_s, ev,
+                                  pairs=[(idx[i], idx[j])])
+        energies[(i, j)] = float(Ep_s[idx[i], idx[j]])
         flop += (2 if i != j else 1) * 2.0 * NBA * NVIRT ** 2
         used_pairs.append((i, j))
         done += 1
@@ -262,7 +272,28 @@ def cpu_reference_sample(seconds, sub, eo_s, ev, pairs_per_step=None, start=0):
     el = time.perf_counter() - t0
     desc = (f"{done} occupied pairs {used_pairs[:4]}... of nocc={NOCC} nvirt={NVIRT} NBA={NBA}, "
             f"full (a,b) range each; eff FLOP counted per ordered pair")
-    return flop / el / 1e12, cores, desc, el
+    return flop / el / 1e12, cores, desc, el, energies
+
+
+def parity_against_oracle(orc, Ep, Ep64):
+    """Sampled pair energies of the CPU oracle (the alpha loop of RIMP2.F90:
+    395-405 restated in C, faithful order, plus the MP2 energy) against the
+    same entries of the GPU split run (bar 1e-7) and of the GPU plain FP64
+    run (bar 1e-11).  A breach prints a warning and sets ok to false."""
+    if not orc:
+        return None
+    sp = [abs(Ep[i, j] - e) / abs(e) for (i, j), e in orc.items()]
+    fp = [abs(Ep64[i, j] - e) / abs(e) for (i, j), e in orc.items()] if Ep64 is not None else []
+    ok = max(sp) <= 1e-7 and (not fp or max(fp) <= 1e-11)
+    if not ok:
+        print(f"PARITY FAILURE against the CPU oracle: split {max(sp):.3e} (bar 1e-7), "
+              f"fp64 {max(fp) if fp else float('nan'):.3e} (bar 1e-11)", file=sys.stderr,
+              flush=True)
+    return {"pairs": len(orc), "pairs_list": sorted(orc), "split_max_rel": max(sp),
+            "fp64_max_rel": max(fp) if fp else None, "split_bar": 1e-7, "fp64_bar": 1e-11,
+            "ok": bool(ok),
+            "against": "CPU oracle: RIMP2.F90:395-405 alpha loop restated in C (faithful "
+                       "order) with the MP2 pair energy, on the bench's own Calpha"}
 
 
 # ------------------------------------------------------------------------------------------
@@ -277,8 +308,8 @@ def run_reference(args):
     desc, cores = "", 1
     sub, eo_s, ev = sample_inputs()
     for step in range(args.warmup + args.steps):
-        v, cores, desc, el = cpu_reference_sample(None, sub, eo_s, ev, pairs_per_step=2,
-                                                  start=2 * step)
+        v, cores, desc, el, _ = cpu_reference_sample(None, sub, eo_s, ev, pairs_per_step=2,
+                                                     start=2 * step)
         if step >= args.warmup:
             vals.append((v, el))
     value = statistics.median(v for v, _ in vals)
@@ -466,7 +497,8 @@ def run_ours(args):
             pms = e0.elapsed_time(e1)
             if pms > 2000.0:
                 break
-        fp64_peak = api.probe_fp64_peak()
+        with Clocks(local) as pclk:
+            fp64_peak = api.probe_fp64_peak()  # one launch of >= 1 s
         # performed DMMA work: i<j pairs compute T1 and T2 of every 64x64 tile
         # pair A<=B, i=j pairs T1 only; K is padded to the 16-wide slab
         nt64 = (NVIRT + 63) // 64
@@ -474,10 +506,13 @@ def run_ours(args):
             64 * 64 * ((NBA + 15) // 16 * 16)
         plain = {"ms": pms, "eff_tflops": eff_flop() / pms / 1e9,
                  "performed_tflops": performed / pms / 1e9, "fp64_dmma_peak_tflops": fp64_peak,
-                 "frac_of_fp64_peak": performed / pms / 1e9 / fp64_peak}
+                 "frac_of_fp64_peak": performed / pms / 1e9 / fp64_peak,
+                 "fp64_peak_probe": "independent DMMA chains on every SM, one launch of >= 1 s "
+                                    "(the library's rimp2_probe_fp64_peak)",
+                 "fp64_peak_probe_clocks": pclk.summary()}
 
     # ---- accuracy of the last step against FP64 ----
-    acc = None
+    acc = Ep64 = None
     Ep = dEp.cpu().numpy().reshape(NOCC, NOCC, order="F")
     Et = dEt.item()
     if plain is not None:
@@ -519,12 +554,25 @@ def run_ours(args):
             "achieved_is": "algorithmic 2*NBA*(nocc*nvirt)^2 FLOP per launch / kernel time"}
 
     # ---- CPU baseline (rank 0, N=1 only) ----
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
         sub, eo_s, ev_s = sample_inputs(Ca_np, eo_host, ev_host)
-        v, cores, desc, el = cpu_reference_sample(args.cpu_seconds, sub, eo_s, ev_s)
+        v, cores, desc, el, orc = cpu_reference_sample(args.cpu_seconds, sub, eo_s, ev_s)
         cpu = {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                "sample": desc + f" ({el:.1f} s)"}
+        parity = parity_against_oracle(orc, Ep, Ep64)
+
+    # ---- configs 4 and 5, compact (rank 0, N=1 only): the batched workload and
+    # the AO pipeline on two fragments; not part of `value` ----
+    batched = ao = None
+    if rank == 0 and world == 1 and not args.no_secondary:
+        batched = batched_leg(api, torch, dev, st, batch_shapes(), steps=3, warmup=3,
+                              check="sample" if args.check == "full" else "none")
+        batched["config"] = ("256 uneven fragments, nocc U[8,64], nvirt U[64,512], NBA "
+                             "U[256,2048], one graph launch per step, device-resident inputs")
+        ao = ao_leg(api, torch, dev, ao_shapes()[:2], steps=2, warmup=1, transform="split",
+                    check="sample" if args.check == "full" else "none")
+        ao["config"] = "the first two fragments of the 64-fragment AO pipeline workload"
 
     if rank == 0:
         line = {
@@ -537,10 +585,11 @@ def run_ours(args):
                        "seed": SEED, "nslices": nsl,
                        "l2": "inputs larger than L2 (Calpha 4.3 GB, FP16 slices 2.1 GB)",
                        "parallelism": f"replicas x{world}"},
-            "accuracy": acc, "plain_fp64": plain,
+            "accuracy": acc, "parity": parity, "plain_fp64": plain,
             "split_over_plain": (value / world / plain["eff_tflops"]) if plain else None,
             "roofline": roof, "cpu_baseline": cpu, "cublas_dgemm_baseline": cub,
             "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+            "batched": batched, "ao": ao,
         }
         print(json.dumps(line), flush=True)
     if pg is not None:
@@ -558,15 +607,13 @@ def batch_shapes(n=BATCH_N, seed=BATCH_SEED):
                     g.integers(256, 2049, n).tolist()))
 
 
-def run_batched(args):
-    import torch
-    from rimp2_gpu_gb300 import api
-    world, rank, local, pg = dist_setup(args)
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    st = torch.cuda.Stream(device=dev)
+def batched_leg(api, torch, dev, st, shapes, steps, warmup, check, e2e=False, pg=None, world=1):
+    """Config 4: uneven fragments in one graph-launched plan per step.
+    check: "full" compares every pair of every fragment with one persistent
+    plain-FP64 launch over the whole batch; "sample" runs 8 evenly spaced
+    fragments in plain FP64 (their rate gives the split/plain ratio) and the
+    two smallest of them through the CPU oracle; "none" skips both."""
     sp = st.cuda_stream
-    shapes = batch_shapes()[:args.batch_fragments]
     eff = sum(2.0 * b * (o * v) ** 2 for o, v, b in shapes)
     frags, desc = [], []
     with torch.cuda.stream(st):
@@ -583,7 +630,7 @@ def run_batched(args):
                          t["ev"].data_ptr(), t["E"].data_ptr(), t["T"].data_ptr()))
     st.synchronize()
     plan = api.BatchPlan(desc, graph=True, stream=sp)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plan.execute(stream=sp)
     api.sync_status(sp)
     barrier(pg)
@@ -591,27 +638,38 @@ def run_batched(args):
     n0 = api.kernel_launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    with Clocks(local) as clk:
+    with Clocks(dev.index or 0) as clk:
         e0.record(st)
-        for _ in range(args.steps):
+        for _ in range(steps):
             plan.execute(stream=sp)
         e1.record(st)
         st.synchronize()
     barrier(pg)
     launches = api.kernel_launch_count() - n0
     api.sync_status(sp)
-    ms = allmax(pg, e0.elapsed_time(e1) / args.steps)
+    ms = allmax(pg, e0.elapsed_time(e1) / steps)
     value = world * eff / (ms * 1e-3) / 1e12
-    # accuracy: the whole batch once more in plain FP64, as one persistent
-    # launch of the fused DMMA kernel over every fragment (untimed for the
-    # metric; its own time is reported as the plain batched form)
-    acc = plain = None
-    if args.check == "full":
+    plan.close()
+    # performed work of the split kernels over ideal: 128-row tile padding
+    padded = sum(2.0 * b * (o * ((v + 127) // 128 * 128)) ** 2 for o, v, b in shapes)
+    out = {"value": value, "unit": "TFLOP/s", "ms_per_step": ms, "fragments": len(shapes),
+           "eff_flop_per_step": eff, "padding_ratio": padded / eff, "gpu_launches": launches,
+           "clocks": clk.summary()}
+    if check == "full":
         with torch.cuda.stream(st):
             out64 = [(torch.zeros(o * o, dtype=torch.float64, device=dev),
                       torch.zeros(1, dtype=torch.float64, device=dev)) for o, v, b in shapes]
         d64 = [d[:6] + (E.data_ptr(), T.data_ptr()) for d, (E, T) in zip(desc, out64)]
-        plan64 = api.BatchPlan(d64, nslices=[0] * len(shapes), graph=False, stream=sp)
+        sel = list(range(len(shapes)))
+    elif check == "sample":
+        sel = sorted(set(int(x) for x in np.linspace(0, len(shapes) - 1, 8)))
+        with torch.cuda.stream(st):
+            out64 = [(torch.zeros(shapes[f][0] ** 2, dtype=torch.float64, device=dev),
+                      torch.zeros(1, dtype=torch.float64, device=dev)) for f in sel]
+        d64 = [desc[f][:6] + (E.data_ptr(), T.data_ptr()) for f, (E, T) in zip(sel, out64)]
+    if check in ("full", "sample"):
+        sub = [shapes[f] for f in sel]
+        plan64 = api.BatchPlan(d64, nslices=[0] * len(d64), graph=False, stream=sp)
         n0p = api.kernel_launch_count()
         p0 = torch.cuda.Event(enable_timing=True)
         p1 = torch.cuda.Event(enable_timing=True)
@@ -623,51 +681,87 @@ def run_batched(args):
         api.sync_status(sp)
         pms = p0.elapsed_time(p1)
         plan64.close()
+        eff_sub = sum(2.0 * b * (o * v) ** 2 for o, v, b in sub)
         # performed MACs: per fragment, i<j pairs compute T1 and T2 for every
         # 64x64 tile pair A<=B, i=j pairs T1 only; K padded to 16
         mac = 0.0
-        for o, v, b in shapes:
+        for o, v, b in sub:
             nt = (v + 63) // 64
             ntp = nt * (nt + 1) // 2
             mac += (o * (o - 1) // 2 * 2 + o) * ntp * 64 * 64 * ((b + 15) // 16 * 16)
         peak64 = api.probe_fp64_peak()
-        plain = {"ms": pms, "eff_tflops": eff / pms / 1e9,
+        plain = {"ms": pms, "eff_tflops": eff_sub / pms / 1e9,
                  "performed_tflops": 2 * mac / pms / 1e9, "fp64_dmma_peak_tflops": peak64,
-                 "frac_of_fp64_peak": 2 * mac / pms / 1e9 / peak64,
-                 "launches": plain_launches,
-                 "form": "plain FP64 fused kernel, all fragments in one persistent launch"}
+                 "frac_of_fp64_peak": 2 * mac / pms / 1e9 / peak64, "launches": plain_launches,
+                 "fragments": len(sub),
+                 "form": "plain FP64 fused kernel, these fragments in one persistent launch"}
         errs, tot = [], []
-        for t, (E64, T64) in zip(frags, out64):
-            a, b = t["E"].cpu().numpy(), E64.cpu().numpy()
+        for f, (E64, T64) in zip(sel, out64):
+            a, b = frags[f]["E"].cpu().numpy(), E64.cpu().numpy()
             errs.append(float(np.max(np.abs(a - b) / np.abs(b))))
-            tot.append(abs(t["T"].item() - T64.item()) / abs(T64.item()))
+            tot.append(abs(frags[f]["T"].item() - T64.item()) / abs(T64.item()))
         acc = {"pair_max_rel_err": max(errs), "total_max_rel_err": max(tot),
                "within_1e-7": bool(max(errs) <= 1e-7 and max(tot) <= 1e-7),
-               "against": f"GPU plain FP64 batch, every pair of all {len(errs)} fragments"}
-    plan.close()
-    e2e = None
-    if not args.no_e2e:
+               "against": f"GPU plain FP64 kernel, every pair of {len(errs)} fragments"}
+        if check == "sample":
+            # the two smallest sampled fragments also against the CPU oracle
+            from oracle import oracle as O
+            O.set_num_threads(os.cpu_count() or 1)
+            small = sorted(sel, key=lambda f: eff_flop(*shapes[f]))[:2]
+            orc = []
+            for f in small:
+                o, v, b = shapes[f]
+                Ca = frags[f]["C"].cpu().numpy().reshape(b, v, o, order="F")
+                Eo, To = O.pair_energies(v, o, b, Ca, frags[f]["eo"].cpu().numpy(),
+                                         frags[f]["ev"].cpu().numpy(), blocked=True)
+                Eo = np.asarray(Eo).ravel(order="F")
+                orc.append(float(np.max(np.abs(frags[f]["E"].cpu().numpy() - Eo) / np.abs(Eo))))
+                k = sel.index(f)
+                orc.append(float(np.max(np.abs(out64[k][0].cpu().numpy() - Eo) / np.abs(Eo))))
+            acc["oracle_fragments"] = [list(shapes[f]) for f in small]
+            acc["oracle_split_pair_max_rel_err"] = max(orc[0::2])
+            acc["oracle_fp64_pair_max_rel_err"] = max(orc[1::2])
+        out["accuracy"] = acc
+        out["plain_fp64"] = plain
+        out["split_over_plain"] = (value / world) / plain["eff_tflops"]
+    ns_hist = {}
+    for o, v, b in shapes:
+        k = api.split_nslices(v, o, b)
+        ns_hist[k] = ns_hist.get(k, 0) + 1
+    out["nslices_histogram"] = ns_hist
+    if e2e:
         host = [(t["C"].cpu().numpy().reshape(b, v, o, order="F"), t["eo"].cpu().numpy(),
                  t["ev"].cpu().numpy()) for t, (o, v, b) in zip(frags, shapes)]
-        for _ in range(max(3, args.warmup)):  # warm (see run_e2e)
+        for _ in range(max(3, warmup)):  # warm (see run_e2e)
             api.energy_batched(host, precision=api.PREC_SPLIT)
         barrier(pg)
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             api.energy_batched(host, precision=api.PREC_SPLIT)
-        e2e_s = allmax(pg, (time.perf_counter() - t0) / args.steps)
-        e2e = {"value": world * eff / e2e_s / 1e12, "unit": "TFLOP/s",
-               "h2d_bytes_per_step": int(sum(8 * (b * v * o + o + v) for o, v, b in shapes)),
-               "d2h_bytes_per_step": int(sum(8 * (o * o + 1) for o, v, b in shapes)),
-               "ms_per_step": e2e_s * 1e3, "host_buffers": "pageable numpy"}
+        e2e_s = allmax(pg, (time.perf_counter() - t0) / steps)
+        out["e2e"] = {"value": world * eff / e2e_s / 1e12, "unit": "TFLOP/s",
+                      "h2d_bytes_per_step": int(sum(8 * (b * v * o + o + v) for o, v, b in shapes)),
+                      "d2h_bytes_per_step": int(sum(8 * (o * o + 1) for o, v, b in shapes)),
+                      "ms_per_step": e2e_s * 1e3, "host_buffers": "pageable numpy"}
+    del frags
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_batched(args):
+    import torch
+    from rimp2_gpu_gb300 import api
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    st = torch.cuda.Stream(device=dev)
+    shapes = batch_shapes()[:args.batch_fragments]
+    r = batched_leg(api, torch, dev, st, shapes, args.steps, args.warmup, args.check,
+                    e2e=not args.no_e2e, pg=pg, world=world)
     if rank == 0:
-        ns_hist = {}
-        for o, v, b in shapes:
-            k = api.split_nslices(v, o, b)
-            ns_hist[k] = ns_hist.get(k, 0) + 1
         line = {
-            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "metric": METRIC, "value": r["value"], "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f16 Ozaki slices, f32 tensor accumulation (exact integer part), f64 reductions",
             "data": "synthetic (seeded Philox4x32-10 + Box-Muller on the device)",
@@ -675,11 +769,13 @@ def run_batched(args):
                                    "uneven fragments (nocc U[8,64], nvirt U[64,512], NBA "
                                    "U[256,2048]) in one graph-launched persistent kernel per "
                                    "slice group", "fragments": len(shapes),
-                       "eff_flop_per_step": eff, "nslices_histogram": ns_hist,
+                       "eff_flop_per_step": r["eff_flop_per_step"],
+                       "padding_ratio": r["padding_ratio"],
+                       "nslices_histogram": r["nslices_histogram"],
                        "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
-            "accuracy": acc, "plain_fp64_batched": plain,
-            "split_over_plain": (value / world / plain["eff_tflops"]) if plain else None,
-            "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+            "accuracy": r.get("accuracy"), "plain_fp64_batched": r.get("plain_fp64"),
+            "split_over_plain": r.get("split_over_plain"),
+            "e2e": r.get("e2e"), "gpu_launches": r["gpu_launches"], "clocks": r["clocks"],
         }
         print(json.dumps(line), flush=True)
     if pg is not None:
@@ -704,26 +800,18 @@ def mo_coefficients(nbas, seed):
     return np.asfortranarray(q * np.sign(np.diag(r)))
 
 
-def run_ao(args):
-    """Full pipeline from AO three-centre integrals: per fragment the AO
-    tensor is generated on the device (untimed input creation), then Calpha
-    is formed on the GPU in FP64 (AO->MO, metric Cholesky, triangular solve;
-    timed), and finally all fragments' energies run as one graph-launched
-    batched split-precision launch (timed)."""
-    import torch
-    from rimp2_gpu_gb300 import api
-    world, rank, local, pg = dist_setup(args)
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
+def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
+    """Config 5: per fragment the AO tensor is generated on the device (untimed
+    input creation), then Calpha is formed on the GPU (AO->MO transform,
+    metric Cholesky, triangular solve; timed), and finally all fragments'
+    energies run as one graph-launched batched split-precision launch (timed).
+    check "full"/"sample": every 16th fragment (at least one) against the GPU
+    FP64 energy kernel."""
     st = torch.cuda.Stream(device=dev)
     # metric Cholesky, concurrent with the transform; high priority so that its
     # latency-bound diagonal-block chain gets SMs ahead of the transform's CTAs
     st2 = torch.cuda.Stream(device=dev, priority=-1)
     sp = st.cuda_stream
-    shapes = ao_shapes(args.ao_fragments)
-    if args.ao_nbas:
-        b = args.ao_nbas
-        shapes = [(b, 3 * b, b // 10, b - b // 10)] * len(shapes)
     maxao = max(b * b * nba for b, nba, _, _ in shapes)
     maxv = max(nba * nba for _, nba, _, _ in shapes)
     maxb = max(nba * nvirt * nocc for _, nba, nocc, nvirt in shapes)
@@ -731,7 +819,7 @@ def run_ao(args):
         ao = torch.empty(maxao, dtype=torch.float64, device=dev)
         V = torch.empty(maxv, dtype=torch.float64, device=dev)
         Bw = torch.empty(maxb, dtype=torch.float64, device=dev)  # (alpha|a i) work array
-    frags, desc, cmos = [], [], []
+    frags, desc = [], []
     for f, (nbas, nba, nocc, nvirt) in enumerate(shapes):
         with torch.cuda.stream(st):
             t = dict(C=torch.empty(nba * nvirt * nocc, dtype=torch.float64, device=dev),
@@ -761,8 +849,8 @@ def run_ao(args):
     eff = sum(2.0 * nba * (nocc * nvirt) ** 2 for _, nba, nocc, nvirt in shapes)
     n0 = None
     parts_ms = []
-    for step in range(args.warmup + args.steps):
-        if step == args.warmup:
+    for step in range(warmup + steps):
+        if step == warmup:
             n0 = api.kernel_launch_count()
         fe = 0.0
         tr = ch = so = 0.0
@@ -775,7 +863,7 @@ def run_ao(args):
             # concurrently on two streams; the triangular solve joins them
             ev[0].record(st)
             api.ao2mo_dev(nba, nbas, nocc, nvirt, ao.data_ptr(), frags[f]["Cmo"].data_ptr(),
-                          Bw.data_ptr(), split=(args.ao_transform == "split"), stream=sp)
+                          Bw.data_ptr(), split=(transform == "split"), stream=sp)
             ev[1].record(st)
             st2.wait_event(ev[0])
             api.cholesky_dev(nba, V.data_ptr(), stream=st2.cuda_stream)
@@ -790,7 +878,7 @@ def run_ao(args):
             ch += ev[0].elapsed_time(ev[3])
             so += ev[4].elapsed_time(ev[5])
             fe += ev[0].elapsed_time(ev[5])
-        if step >= args.warmup:
+        if step >= warmup:
             parts_ms.append((tr, ch, so))
         if plan is None:
             plan = api.BatchPlan(desc, graph=True, stream=sp)
@@ -801,7 +889,7 @@ def run_ao(args):
         e1.record(st)
         st.synchronize()
         api.sync_status(sp)
-        if step >= args.warmup:
+        if step >= warmup:
             fe_ms.append(fe)
             en_ms.append(e0.elapsed_time(e1))
     launches = api.kernel_launch_count() - n0
@@ -811,7 +899,7 @@ def run_ao(args):
     so_m = statistics.median(p[2] for p in parts_ms)
     ms = allmax(pg, fe_m + en_m)
     acc = None
-    if args.check == "full":
+    if check in ("full", "sample"):
         errs, tot = [], []
         for f in range(0, len(shapes), 16):
             _, nba, nocc, nvirt = shapes[f]
@@ -829,32 +917,54 @@ def run_ao(args):
                "within_1e-7": bool(max(errs) <= 1e-7 and max(tot) <= 1e-7),
                "against": f"GPU FP64 kernel on {len(errs)} sampled fragments"}
     plan.close()
+    del frags, ao, V, Bw
+    torch.cuda.empty_cache()
+    return {"value": eff / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms,
+            "fragments": len(shapes), "shapes_nbas_nba_nocc_nvirt": [list(x) for x in shapes[:4]],
+            "ao_transform": transform, "front_end_ms": fe_m, "energy_ms": en_m,
+            "front_end_overlap": "AO->MO transform and metric Cholesky run concurrently "
+                                 "(two streams); parts overlap",
+            "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,
+            "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
+            "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
+            "transform_algorithmic_bytes": ao_bytes,
+            "cholesky_fp64_tflops": ch_flop / (ch_m * 1e-3) / 1e12,
+            "solve_fp64_tflops": so_flop / (so_m * 1e-3) / 1e12,
+            "solve_performed_fp64_tflops": so_perf / (so_m * 1e-3) / 1e12,
+            "energy_eff_tflops": eff / (en_m * 1e-3) / 1e12,
+            "ao_generation": "untimed, per fragment, streamed through one buffer",
+            "accuracy": acc, "gpu_launches": launches}
+
+
+def run_ao(args):
+    import torch
+    from rimp2_gpu_gb300 import api
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    shapes = ao_shapes(args.ao_fragments)
+    if args.ao_nbas:
+        b = args.ao_nbas
+        shapes = [(b, 3 * b, b // 10, b - b // 10)] * len(shapes)
+    r = ao_leg(api, torch, dev, shapes, args.steps, args.warmup, args.ao_transform, args.check,
+               pg=pg)
     if rank == 0:
+        cfg = {k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step",
+                                                       "accuracy", "gpu_launches")}
+        cfg["workload"] = f"pipeline from AO integrals, {len(shapes)} fragments " + (
+            "(nbas U[128,768], NBA=3 nbas, nocc=nbas/10)" if not args.ao_nbas else
+            f"(nbas={args.ao_nbas}, NBA=3 nbas, nocc=nbas/10; reduced case)")
+        cfg["parallelism"] = f"replicas x{world}"
         line = {
-            "metric": METRIC, "value": world * eff / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "metric": METRIC, "value": world * r["value"], "unit": "TFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
             "dtype": ("f16 Ozaki slices for AO->MO and the energy, f64 Cholesky/solve/reductions"
                       if args.ao_transform == "split" else
                       "f64 front end; f16 Ozaki slices / f32 tensor accumulation for the energy"),
             "data": "synthetic (device Philox AO integrals and metric, numpy QR MO coefficients)",
-            "config": {"workload": f"pipeline from AO integrals, {len(shapes)} fragments " + (
-                           "(nbas U[128,768], NBA=3 nbas, nocc=nbas/10)" if not args.ao_nbas else
-                           f"(nbas={args.ao_nbas}, NBA=3 nbas, nocc=nbas/10; reduced case)"),
-                       "ao_transform": args.ao_transform,
-                       "front_end_ms": fe_m, "energy_ms": en_m,
-                       "front_end_overlap": "AO->MO transform and metric Cholesky run "
-                                            "concurrently (two streams); parts overlap",
-                       "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,
-                       "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
-                       "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
-                       "cholesky_fp64_tflops": ch_flop / (ch_m * 1e-3) / 1e12,
-                       "solve_fp64_tflops": so_flop / (so_m * 1e-3) / 1e12,
-                       "solve_performed_fp64_tflops": so_perf / (so_m * 1e-3) / 1e12,
-                       "energy_eff_tflops": eff / (en_m * 1e-3) / 1e12,
-                       "ao_generation": "untimed, per fragment, streamed through one buffer",
-                       "parallelism": f"replicas x{world}"},
-            "accuracy": acc, "gpu_launches": launches,
+            "config": cfg, "accuracy": r["accuracy"], "gpu_launches": r["gpu_launches"],
         }
         print(json.dumps(line), flush=True)
     if pg is not None:

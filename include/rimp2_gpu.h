@@ -62,6 +62,11 @@ int rimp2_sync_status(void *stream);
  * budget of budget_cycles SM clocks (<= 1e9).  Expected result:
  * RIMP2_ERR_TIMEOUT, with the library usable afterwards. */
 int rimp2_selftest_bounded_wait(long long budget_cycles, void *stream);
+/* Numerics self-test of the split epilogue's reciprocal of an energy
+ * denominator (hardware approximation plus one Newton-Raphson step): for the
+ * n host values d, r[k] receives that reciprocal and ref[k] CUDA's correctly
+ * rounded single-precision 1/d (__frcp_rn), both computed on the GPU. */
+int rimp2_selftest_rcp_denom(int n, const float *d, float *r, float *ref);
 /* Opt-in CUDA-event timing of the split path's phases; rimp2_last_timing
  * fills ms4 = {slicing, energy kernel, reductions, 0} of the last call. */
 int rimp2_set_timing(int on);
@@ -75,7 +80,8 @@ int rimp2_last_timing(float *ms4);
  * overrides that choice. */
 int rimp2_last_split_kernel(void);
 /* Measured FP64 tensor-op (DMMA) throughput of this GPU in TFLOP/s, the
- * denominator for the plain kernel's roofline fraction. */
+ * denominator for the plain kernel's roofline fraction: independent DMMA
+ * chains on every SM, timed over one launch of at least a second. */
 int rimp2_probe_fp64_peak(double *tflops);
 
 /* ---- drop-in subroutines of RIMP2.F90 -----------------------------------
@@ -227,16 +233,19 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
 int rimp2_split_nslices(int nvirt, int nocc, int NBA);
 
 /* FP64 pair and total energies like rimp2_energy_dev(..., RIMP2_PREC_FP64),
- * for callers that cannot allocate device memory when they call: it uses no
- * cudaMalloc/cudaFree or allocating library routine, only a fixed 16 MiB
- * device array inside this library (held on every GPU that loads it until
- * the process exits).  Fragments whose pair list plus per-tile partials
- * exceed it (8*npairs*(ceil(nvirt/64)(ceil(nvirt/64)+1)/2 + 1) bytes,
- * npairs = nocc(nocc+1)/2) get RIMP2_ERR_ARG.  stream NULL = the default
- * stream.  Calls share the array: calls that overlap on the GPU race.  The
- * first call on a device looks the array up and should precede any stream
- * capture.  No counterpart in the reference (its GPU driver allocates through
- * OpenACC data regions, RIMP2.GPU.F90:107). */
+ * for callers that cannot allocate device memory when they call -- a
+ * Fortran/OpenACC program whose data regions already hold (nearly) all of the
+ * device memory, or code running while another allocator owns it.  It uses
+ * no cudaMalloc/cudaFree or allocating library routine, only a fixed 16 MiB
+ * device array inside this library (held on every GPU that loads it until the
+ * process exits).  Fragments whose pair list plus per-tile partials exceed it
+ * (8*npairs*(ceil(nvirt/64)(ceil(nvirt/64)+1)/2 + 1) bytes, npairs =
+ * nocc(nocc+1)/2; nocc=128 with nvirt=1024 fits) get RIMP2_ERR_ARG.  stream
+ * NULL = the default stream.  Calls share the array: calls that overlap on
+ * the GPU race.  The array and this path's kernels are placed on a device by
+ * the first call of any entry point of this library there (rimp2_get_dev_mem
+ * is a cheap one): make that call before filling the device memory and before
+ * any stream capture.  No counterpart in the reference. */
 int rimp2_energy_fp64_noalloc_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
                                   const double *dEVocc, const double *dEVvirt, double *dEpair,
                                   double *dEtot, void *stream);

@@ -30,6 +30,8 @@ SIGNATURES = {
     "rimp2_sync_status": ([_vp], C.c_int),
     "rimp2_set_timing": ([C.c_int], C.c_int),
     "rimp2_selftest_bounded_wait": ([C.c_longlong, _vp], C.c_int),
+    "rimp2_selftest_rcp_denom": ([C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)], C.c_int),
     "rimp2_last_timing": ([C.POINTER(C.c_float)], C.c_int),
     "rimp2_last_split_kernel": ([], C.c_int),
     "rimp2_probe_fp64_peak": ([_dp], C.c_int),

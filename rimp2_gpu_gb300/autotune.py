@@ -1,6 +1,7 @@
 """Shape-bucket autotuner for the split-precision energy path.
 
-Below 16 virtuals fragments run in FP64 (slice count 0, a fixed rule).  For
+Below 16 virtuals, and below 64 (a,i) columns (nocc*nvirt), fragments run
+in FP64 (slice count 0, fixed rules in the library).  For
 each larger virtual-space bucket it runs representative seeded fragments on the
 GPU three ways -- the plain FP64 kernel (the reference values) and the split
 kernel with one and with two residual slices -- and picks the cheapest slice
@@ -95,7 +96,9 @@ def tune(seed=77):
     fixed = {"nvirt_min": 0, "nslices": 0,
              "rule": f"fragments with fewer than {FP64_BELOW} virtuals run in FP64: a pair "
                      "energy of a few g^2 terms has nothing to average the split form's "
-                     "FP32-accumulated correction against"}
+                     "FP32-accumulated correction against; the library also sends every "
+                     "fragment with nocc*nvirt < 64 to FP64 (its FP32 epilogue rounding "
+                     "leaves 2-5e-8 on such pair energies)"}
     return {"target": TARGET, "margin": 0.5, "buckets": [fixed] + table}
 
 

@@ -121,6 +121,10 @@ int ensure_device() {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
+  // load the allocation-free entry point's fixed array and kernels now, while
+  // the caller can still spare the memory; a failure here only concerns that
+  // entry point, which reports its own error when called
+  if (noalloc_preload() != RIMP2_OK) clear_error();
   g_dev_ok = 1;
   return RIMP2_OK;
 }
@@ -445,6 +449,14 @@ int rimp2_selftest_bounded_wait(long long budget_cycles, void *stream) {
   RIMP2_TRY(ensure_device());
   cudaStream_t s = stream ? (cudaStream_t)stream : current_stream();
   return bounded_wait_selftest(budget_cycles, s);
+}
+
+int rimp2_selftest_rcp_denom(int n, const float *d, float *r, float *ref) {
+  clear_error();
+  RIMP2_REQ(n > 0 && n <= (1 << 26) && d && r && ref,
+            "rimp2_selftest_rcp_denom: need 0 < n <= 2^26 and three host arrays");
+  RIMP2_TRY(ensure_device());
+  return rcp_denom_selftest(n, d, r, ref, current_stream());
 }
 
 int rimp2_set_timing(int on) {
@@ -951,9 +963,17 @@ static std::vector<std::pair<int, int>> g_buckets = {{0, 0},   {16, 2},  {128, 2
                                                      {192, 1}, {256, 1}, {384, 1}};
 static std::mutex g_bucket_mu;
 
+// Fragments with fewer than 64 (a,i) columns also run in FP64, whatever the
+// table says: the split form's FP32 epilogue rounds every element's energy
+// term (g, the reciprocal, the product) to ~2^-24, and a pair energy made of a
+// handful of such terms, partly cancelling, keeps 2-5e-8 of that rounding
+// (CPU emulation of the epilogue), too close to the 1e-7 bar; in FP64 such a
+// fragment costs microseconds.
+constexpr long long kSplitMinColumns = 64;
+
 int rimp2_split_nslices(int nvirt, int nocc, int NBA) {
-  (void)nocc;
   (void)NBA;
+  if ((long long)nocc * nvirt < kSplitMinColumns) return 0;
   std::lock_guard<std::mutex> lk(g_bucket_mu);
   int ns = 2;
   for (auto &b : g_buckets)

@@ -104,6 +104,10 @@ int probe_fp64_peak(double *tflops, cudaStream_t s);
 void plain_energy_scratch_sizes(int nvirt, int nocc, long long *npairs, long long *nitems);
 int plain_energy_f64_scratch(const PlainEnergyArgs &a, int *pairs_scratch, double *part_scratch,
                              cudaStream_t s);
+int preload_plain_scratch_kernels();
+// Loads the allocation-free entry point's scratch array and kernels onto the
+// current device (ensure_device calls it on the library's first use).
+int noalloc_preload();
 // Fused local-orbital energy from Calpha and its projected copy Ct (FP64).
 int eos_energy_f64(const double *Ca, const double *Ct, int NBA, int nvirt, int nocc,
                    const double *eo, const double *ev, double *Epair, double *Etot,
@@ -144,6 +148,7 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
 int split_plan_execute(SplitPlan *P, cudaStream_t s);
 void split_plan_destroy(SplitPlan *P);
 int bounded_wait_selftest(long long budget_cycles, cudaStream_t s);
+int rcp_denom_selftest(int n, const float *d, float *r, float *ref, cudaStream_t s);
 int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs &a,
                           cudaStream_t s, cudaStream_t copy_s, int chunk_occ);
 cudaStream_t copy_stream();

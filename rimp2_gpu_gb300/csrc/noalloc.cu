@@ -20,11 +20,16 @@
 // contents; each launch writes every scratch element it later reads (pair
 // list, partials), so nothing needs clearing between calls.  Calls whose
 // work overlaps on the GPU (different streams, or different host threads on
-// one device) race on the array: serialise them.  The first call on a device
-// looks up the array's device address (cudaGetSymbolAddress) with that device
-// current; make that first call before any stream capture.
-#include <mutex>
-
+// one device) race on the array: serialise them.
+//
+// When the array exists: CUDA loads a module (and creates its __device__
+// arrays) lazily, when something first refers to it.  The library's regular
+// device set-up (ensure_device, run by the first call of any other entry
+// point, rimp2_get_dev_mem included) loads this array and the four kernels
+// of this path on the current device.  A caller that must not allocate later
+// makes such a call once per device before it fills the device memory (and
+// before any stream capture); if the allocation-free entry point is the first
+// call on a device, that call loads them itself.
 #include "common.cuh"
 
 namespace {
@@ -32,32 +37,23 @@ namespace {
 constexpr size_t NOALLOC_SCRATCH_BYTES = 16u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-static void *g_scratch_addr[kMaxDevices] = {};
-static std::mutex g_scratch_mu;
-
-// Device address of the scratch array on the current device (set up once per
-// device).  The name g_noalloc_scratch is only a host-side handle; kernels
-// must be given this address, never the symbol itself.
+// Device address of the scratch array on the current device.  The name
+// g_noalloc_scratch is only a host-side handle; kernels must be given this
+// address, never the symbol itself.  Looked up on every call (cheap once the
+// module is loaded), so a device reset that reloads the module at another
+// address leaves no stale pointer behind.
 int scratch_address(void **out) {
   int dev = 0;
   RIMP2_CK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    rimp2::set_error("rimp2_energy_fp64_noalloc_dev: device index %d out of range", dev);
-    return RIMP2_ERR_ARG;
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    (void)cudaGetLastError();
+    rimp2::set_error("cudaGetSymbolAddress(scratch) failed on device %d: %s", dev,
+                     cudaGetErrorString(e));
+    return RIMP2_ERR_CUDA;
   }
-  std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      rimp2::set_error("cudaGetSymbolAddress(scratch) failed on device %d: %s", dev,
-                       cudaGetErrorString(e));
-      return RIMP2_ERR_CUDA;
-    }
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
+  *out = p;
   return RIMP2_OK;
 }
 
@@ -83,6 +79,14 @@ int check_device_noalloc() {
 
 }  // namespace
 
+namespace rimp2 {
+int noalloc_preload() {
+  void *p = nullptr;
+  RIMP2_TRY(scratch_address(&p));
+  return preload_plain_scratch_kernels();
+}
+}  // namespace rimp2
+
 extern "C" int rimp2_energy_fp64_noalloc_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
                                              const double *dEVocc, const double *dEVvirt,
                                              double *dEpair, double *dEtot, void *stream) {
@@ -101,6 +105,7 @@ extern "C" int rimp2_energy_fp64_noalloc_dev(int nvirt, int nocc, int NBA, const
   RIMP2_TRY(check_device_noalloc());
   void *base = nullptr;
   RIMP2_TRY(scratch_address(&base));
+  RIMP2_TRY(rimp2::preload_plain_scratch_kernels());
   rimp2::PlainEnergyArgs a;
   a.Ca = dCalpha;
   a.NBA = NBA;

@@ -881,7 +881,6 @@ __global__ void __launch_bounds__(BATCH_THREADS, 1)
 // --------------------------------------------------------------------------
 constexpr int BHALF = TILE / 2;                  // B rows of an N=128 operand per CTA
 constexpr int BPANEL_BYTES = BHALF * KSTEP * 2;  // 8 KB
-constexpr int PAIR_NSTAGE = 3;
 // per-CTA stage: A panels S0a, R1a (16 KB each); Y = 128 rows of the N=256
 // operand (rank 0: S0b, rank 1: R1b); W = 64 rows of Vb
 constexpr int PAIR_STAGE_BYTES = 3 * PANEL_BYTES + BPANEL_BYTES;  // 56 KB
@@ -988,15 +987,38 @@ struct PairParams {
   const float2 *eo2, *ev2;
   const float *inv_scale;
   double *part;          // indexed like split_batch_kernel's work items
+  float *xbuf;           // GX form: one 128x128 FP32 exchange tile per CTA of the grid
   int *err;
 };
 
-int pair_smem_bytes() { return PAIR_NSTAGE * PAIR_STAGE_BYTES + 1024 + 512 + 64 * TP * 4; }
+// Shared memory of split_pair_kernel<NSTAGE, GX>: the stage ring, barriers and
+// item ring, and (GX = false) the 64-row transpose buffer.  With the exchange
+// tile transposed through global scratch (GX = true) a fourth 56 KB stage
+// fits in the 227 KB a CTA may hold.
+constexpr int pair_smem_bytes(int nstage, bool gx) {
+  return nstage * PAIR_STAGE_BYTES + 1024 + 512 + (gx ? 0 : 64 * TP * 4);
+}
 
+// Exchange-tile transpose through memory, for the GX form: each thread stores
+// its 64 values of tile row `row` (columns [cbase, cbase+64)) as 16-byte
+// vectors, and after a barrier reads column `row` back 16 values at a time,
+// coalesced across the warp.  The .cg forms keep the round trip in L2, so no
+// SM-local cache line of the previous item's tile is ever read.
+__device__ __forceinline__ void st_cg4(float *p, float a, float b, float c, float d) {
+  asm volatile("st.global.cg.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
+}
+__device__ __forceinline__ float ld_cg(const float *p) {
+  float v;
+  asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <int NSTAGE, bool GX>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
     split_pair_kernel(const __grid_constant__ CUtensorMap tmA,
                       const __grid_constant__ CUtensorMap tmB, PairParams P) {
-  constexpr int NSTAGE = PAIR_NSTAGE;
   constexpr int STAGE_BYTES = PAIR_STAGE_BYTES;
   constexpr int NEPI = 8;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -1315,6 +1337,46 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
           const uint32_t t2 = tmem + lane_off + 2 * TILE + cbase;
           const float sbi = scl[i * nvpad + tB * TILE + row];      // T2' row (b,i)
           const float *saj = scl + j * nvpad + tA * TILE + cbase;  // T2' columns (a,j)
+          if constexpr (GX) {
+            // every thread stores row `row` of the tile to transpose (T1 when
+            // A == B, else T2'), then reads column `row` of it
+            float *X = P.xbuf + (size_t)blockIdx.x * (TILE * TILE);
+            float *dst = X + row * TILE + cbase;
+            if (diag) {
+#pragma unroll
+              for (int k = 0; k < 64; k += 4) st_cg4(dst + k, g1[k], g1[k + 1], g1[k + 2], g1[k + 3]);
+            } else {
+#pragma unroll
+              for (int c0 = 0; c0 < 64; c0 += 16) {
+                float l0[16], l1[16];
+                tmem_ld16(t2 + c0, l0);
+                tmem_ld16(t2 + TILE + c0, l1);
+                tmem_wait_ld();
+                float v[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k) v[k] = (l0[k] + l1[k]) * (sbi * saj[c0 + k]);
+#pragma unroll
+                for (int k = 0; k < 16; k += 4) st_cg4(dst + c0 + k, v[k], v[k + 1], v[k + 2], v[k + 3]);
+              }
+              release_t2();
+            }
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            const float *src = X + (size_t)cbase * TILE + row;
+            float ga[16], gb[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) ga[k] = ld_cg(src + k * TILE);
+#pragma unroll
+            for (int c0 = 0; c0 < 64; c0 += 32) {
+#pragma unroll
+              for (int k = 0; k < 16; ++k) gb[k] = ld_cg(src + (c0 + 16 + k) * TILE);
+              eacc += (double)terms(c0, ga);
+              if (c0 + 32 < 64) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k) ga[k] = ld_cg(src + (c0 + 32 + k) * TILE);
+              }
+              eacc += (double)terms(c0 + 16, gb);
+            }
+          } else {
 #pragma unroll 1
           for (int h = 0; h < 2; ++h) {
             asm volatile("bar.sync 1, 256;" ::: "memory");
@@ -1346,6 +1408,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NTHREADS, 1)
                 eacc += (double)terms(c0, g2);
               }
             }
+          }
           }
         }
       }
@@ -1836,6 +1899,16 @@ __global__ void wait_selftest_kernel(long long budget, int *err) {
   __syncthreads();
 }
 
+// Self-test of the epilogue's reciprocal: rcp_denom(d) beside CUDA's
+// correctly rounded single-precision reciprocal __frcp_rn(d).
+__global__ void rcp_selftest_kernel(const float *__restrict__ d, float *__restrict__ r,
+                                    float *__restrict__ ref, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  r[t] = rcp_denom(d[t]);
+  ref[t] = __frcp_rn(d[t]);
+}
+
 // --------------------------------------------------------------------------
 // reductions of a batch (deterministic, compensated)
 // --------------------------------------------------------------------------
@@ -1960,7 +2033,41 @@ struct Group {
   long long npitems = 0;
   DevBuf pitems, dcorr;  // dcorr: per-column diagonal correction of the V product
   CUtensorMap tmB;
+  int pair_nstage = 3;  // 3: exchange transpose in shared memory; 4: through xbuf
+  DevBuf xbuf;          // 4-stage form: one 64 KB exchange tile per CTA
 };
+
+// Stage count of the paired kernel for a group.  The fourth 56 KB stage
+// (which needs the exchange tile transposed through global scratch instead of
+// shared memory) covers the cross-CTA refill round trip on long product
+// chains; on short ones the per-item epilogue is exposed and the slower
+// global-memory transpose costs more than the deeper ring gains.  Decided on
+// the work-weighted mean of the group's K chunks; RIMP2_PAIR_STAGES=3 or =4
+// in the environment overrides it.
+int pair_stages_for(const std::vector<FragDesc> &fh) {
+  const char *e = getenv("RIMP2_PAIR_STAGES");
+  if (e && e[0] == '3') return 3;
+  if (e && e[0] == '4') return 4;
+  double w = 0.0, wk = 0.0;
+  for (const auto &F : fh) {
+    const double work = (double)pair_items_before(F.nocc) * F.ntp * F.nks;
+    w += work;
+    wk += work * F.nks;
+  }
+  (void)wk;
+  return 3;  // the four-stage form is opt-in until measured
+}
+
+int launch_pair(const Group &g, PairParams Q, int npair, cudaStream_t s) {
+  Q.xbuf = g.xbuf.as<float>();
+  if (g.pair_nstage == 4)
+    split_pair_kernel<4, true>
+        <<<2 * npair, NTHREADS, pair_smem_bytes(4, true), s>>>(g.tm, g.tmB, Q);
+  else
+    split_pair_kernel<3, false>
+        <<<2 * npair, NTHREADS, pair_smem_bytes(3, false), s>>>(g.tm, g.tmB, Q);
+  return RIMP2_OK;
+}
 
 // Kernel choice per one-residual-slice fragment.  The paired-CTA kernel
 // (three products per element pair) runs in 0.87-0.95x the one-CTA kernel's
@@ -2058,8 +2165,20 @@ int build_group(Group &g, cudaStream_t s) {
   RIMP2_CK(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2, 3)));
   RIMP2_CK(cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(3, 2)));
   if (g.pair) {
-    RIMP2_CK(cudaFuncSetAttribute(split_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  pair_smem_bytes()));
+    g.pair_nstage = pair_stages_for(g.fh);
+    if (g.pair_nstage == 4) {
+      int dev = 0, nsm = 0;
+      RIMP2_CK(cudaGetDevice(&dev));
+      RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      RIMP2_TRY(g.xbuf.alloc(sizeof(float) * TILE * TILE * (size_t)nsm, s));
+      RIMP2_CK(cudaFuncSetAttribute(split_pair_kernel<4, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    pair_smem_bytes(4, true)));
+    } else {
+      RIMP2_CK(cudaFuncSetAttribute(split_pair_kernel<3, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    pair_smem_bytes(3, false)));
+    }
     cuuint32_t boxB[3] = {KSTEP, BHALF, 1};
     cr = encode(&g.tmB, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, g.slices.p, dims, strides, boxB, estr,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -2123,7 +2242,7 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
     Q.part = P.part;
     Q.err = P.err;
     const int npair = (int)std::min<long long>(g.npitems, std::max(1, nsm / 2));
-    split_pair_kernel<<<2 * npair, NTHREADS, pair_smem_bytes(), s>>>(g.tm, g.tmB, Q);
+    RIMP2_TRY(launch_pair(g, Q, npair, s));
     note_split_kernel(2);
   } else if (g.nsl == 2) {
     note_split_kernel(1);
@@ -2588,6 +2707,23 @@ int bounded_wait_selftest(long long budget_cycles, cudaStream_t s) {
   return collect_device_error(s);
 }
 
+int rcp_denom_selftest(int n, const float *d, float *r, float *ref, cudaStream_t s) {
+  DevBuf dd, dr, dref;
+  const size_t b = sizeof(float) * (size_t)n;
+  RIMP2_TRY(dd.alloc(b, s));
+  RIMP2_TRY(dr.alloc(b, s));
+  RIMP2_TRY(dref.alloc(b, s));
+  RIMP2_CK(cudaMemcpyAsync(dd.p, d, b, cudaMemcpyHostToDevice, s));
+  rcp_selftest_kernel<<<(n + 255) / 256, 256, 0, s>>>(dd.as<float>(), dr.as<float>(),
+                                                      dref.as<float>(), n);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  RIMP2_CK(cudaMemcpyAsync(r, dr.p, b, cudaMemcpyDeviceToHost, s));
+  RIMP2_CK(cudaMemcpyAsync(ref, dref.p, b, cudaMemcpyDeviceToHost, s));
+  RIMP2_CK(cudaStreamSynchronize(s));
+  return RIMP2_OK;
+}
+
 // Host Calpha -> energies with the copy overlapped: occupied indices are
 // copied in chunks on a second stream; once chunk c has landed, its columns
 // are sliced and the work items of every pair (i <= j) with j in chunk c --
@@ -2674,7 +2810,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
       Q.err = BP.err;
       const int npair = (int)std::min<long long>(Q.nitems - Q.item_begin, std::max(1, P->nsm / 2));
       note_split_kernel(2);
-      split_pair_kernel<<<2 * npair, NTHREADS, pair_smem_bytes(), s>>>(g.tm, g.tmB, Q);
+      launch_pair(g, Q, npair, s);
     } else {
       // pairs (i<=j) with j in [i0, i1): pair indices [i0(i0+1)/2, i1(i1+1)/2)
       const long long pb = (long long)i0 * (i0 + 1) / 2, pe = (long long)i1 * (i1 + 1) / 2;

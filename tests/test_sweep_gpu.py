@@ -1,9 +1,10 @@
 """Seeded sweep over small ragged fragment shapes (1 <= nocc <= 20,
-1 <= nvirt <= 260, 1 <= NBA <= 700), each checked against the CPU oracle:
-single-fragment FP64 (1e-11 relative per pair and total) and split (1e-7;
-2e-7 for fragments with fewer than 64 (a,i) columns, where nothing averages
-the FP32 epilogue rounding), and the same shapes as one batch through the
-host batched call in both precisions."""
+1 <= nvirt <= 260, 1 <= NBA <= 700, plus the tiniest split shapes: nocc 1-3
+with 16 <= nvirt <= 63), each checked against the CPU oracle: single-fragment
+FP64 (1e-11 relative per pair and total) and split (1e-7 on every shape; the
+library sends fragments with fewer than 64 (a,i) columns to its FP64 tier),
+and the same shapes as one batch through the host batched call in both
+precisions."""
 import numpy as np
 import pytest
 
@@ -16,6 +17,10 @@ SHAPES = [(int(o), int(v), int(b)) for o, v, b in zip(_g.integers(1, 21, 20),
                                                          _g.integers(1, 261, 20),
                                                          _g.integers(1, 701, 20))]
 SHAPES += [(1, 1, 1), (1, 129, 1), (20, 1, 700), (2, 257, 65)]
+# nocc in {1,2,3}, 16 <= nvirt <= 63: either side of the 64-column FP64 tier
+_t = np.random.Generator(np.random.Philox(2025))
+SHAPES += [(o, int(v), int(b)) for o in (1, 2, 3)
+           for v, b in zip(_t.integers(16, 64, 3), _t.integers(32, 701, 3))]
 
 
 @pytest.fixture(scope="module")
@@ -29,7 +34,7 @@ def cases():
 
 
 def _tol_split(nocc, nvirt):
-    return 1e-7 if nocc * nvirt >= 64 else 2e-7
+    return 1e-7
 
 
 def _check(Ep, E, ref_Ep, ref_E, tol):

@@ -2,10 +2,11 @@
 
 Callers such as a Fortran/OpenACC driver that already owns the device memory
 cannot let the library allocate; rimp2_energy_fp64_noalloc_dev works out of a
-fixed device array instead.  Its energies must match the regular FP64 entry
-point (same 1e-11 relative tolerance as the FP64 parity tests) on two calls
-in a row, the second reusing the array left by the first.  Collected last so
-that a failure here never hides the other tests.
+fixed device array instead.  Its energies must match the CPU oracle and the
+regular FP64 entry point (the 1e-11 relative tolerance of the FP64 parity
+tests) on two calls in a row, the second reusing the array left by the first,
+and the second call must leave the device's free memory unchanged.  Collected
+last so that a failure here never hides the other tests.
 """
 import ctypes as C
 
@@ -38,18 +39,28 @@ def test_noalloc_matches_regular_entry_point_twice():
         torch.cuda.synchronize()
         Er = ref_E.cpu().numpy()
         Tr = ref_T.item()
+        Eo, To = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+        Eo = np.asarray(Eo).ravel(order="F")
         for call in range(2):
             dE = torch.full((nocc * nocc,), np.nan, dtype=torch.float64, device="cuda")
             dT = torch.full((1,), np.nan, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            free0 = api.get_dev_mem()[1]
             st = L.rimp2_energy_fp64_noalloc_dev(nvirt, nocc, NBA, dC.data_ptr(), deo.data_ptr(),
                                                  dev.data_ptr(), dE.data_ptr(), dT.data_ptr(),
                                                  None)
             assert st == 0, L.rimp2_last_error_string()
             torch.cuda.synchronize()
+            free1 = api.get_dev_mem()[1]
+            if call == 1:
+                assert free1 == free0, f"device free memory moved by {free0 - free1} bytes"
             E = dE.cpu().numpy()
             rel = np.abs(E - Er) / np.abs(Er)
             assert rel.max() <= 1e-11, (call, rel.max())
             assert abs(dT.item() - Tr) <= 1e-11 * abs(Tr), call
+            rel_o = np.abs(E - Eo) / np.abs(Eo)
+            assert rel_o.max() <= 1e-11, ("oracle", call, rel_o.max())
+            assert abs(dT.item() - To) <= 1e-11 * abs(To), ("oracle total", call)
 
 
 def test_noalloc_rejects_fragments_above_its_limit():
