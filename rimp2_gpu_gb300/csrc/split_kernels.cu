@@ -262,37 +262,10 @@ __device__ __forceinline__ void decode_tri(int q, int &A, int &B) {
 // and padded K are zero); inv_scale[col] = 2^-e.
 //
 // GB300 runs FP64 arithmetic at a small fraction of its FP32 rate, so the
-// per-element work here avoids the FP64 pipe: the double is split into an
-// exact float pair (xh, xl) by bit manipulation, with the power-of-two scale
-// applied to the exponent field, and rounding/residuals are taken in FP32
-// where they are exact or carry ~2^-48 relative error.  Only the per-column
-// scale choice uses FP64.
-__device__ __forceinline__ float bits_to_float_trunc(unsigned long long b, int add_exp) {
-  // double bits -> float with truncated mantissa, exponent shifted by add_exp;
-  // caller guarantees the result is a normal float or zero
-  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-  if (mag == 0) return 0.0f;
-  const int ex = (int)(mag >> 52) - 1023 + add_exp;
-  if (ex < -126) return 0.0f;  // below float range: negligible against |C*s| <= 2048
-  if (ex > 127) return __uint_as_float(((uint32_t)(b >> 63) << 31) | 0x7F800000u);
-  const uint32_t mant = (uint32_t)((mag >> 29) & 0x7FFFFFu);
-  const uint32_t sign = (uint32_t)(b >> 63) << 31;
-  return __uint_as_float(sign | ((uint32_t)(ex + 127) << 23) | mant);
-}
-
-__device__ __forceinline__ void split_double(double c, int e, float &xh, float &xl) {
-  // x = c * 2^e = xh + xl, xh = x truncated to 24 bits, xl = rest (rounded to 24 bits)
-  const unsigned long long b = (unsigned long long)__double_as_longlong(c);
-  xh = bits_to_float_trunc(b, e);
-  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-  const int ex = (int)(mag >> 52) - 1023 + e;
-  const unsigned long long low = mag & 0x1FFFFFFFull;  // 29 mantissa bits below xh
-  float l = (float)(unsigned int)low;                  // exact to 24 bits
-  l = ldexpf(l, ex - 52);
-  xl = (b >> 63) ? -l : l;
-  if (mag == 0 || ex < -126) xl = 0.0f;
-}
-
+// per-element work here avoids the FP64 pipe: the scaled value's integer
+// part and remainder come from the mantissa bits by integer arithmetic
+// (split_int below), the remainder is then rounded to FP16 slices in FP32.
+// Only the per-column scale choice uses FP64, in one thread per column.
 // One fragment of a batch: sizes, where its data lives, where its slices,
 // scales, work items and pair energies go.
 struct FragDesc {
@@ -330,11 +303,77 @@ __device__ __forceinline__ void decode_pair(int p, int &i, int &j) {
   i = p - jj * (jj + 1) / 2;
 }
 
+// Per-element arithmetic of the slicing kernels in 32/64-bit integer
+// operations on the FP64 bit pattern: GB300's FP64 pipe is far too slow for
+// per-element work, and assembling floats with ldexpf costs several times
+// more instructions (the slicing kernels are issue-bound, ncu).
+//
+// |v| truncated to float (mantissa cut to 24 bits), for a column's sum of
+// squares: the exponent is rebiased in place; values below the float range
+// count as 0, values above it as FLT_MAX.
+__device__ __forceinline__ float abs_trunc_f32(unsigned long long mag) {
+  const unsigned int ed = (unsigned int)(mag >> 52);
+  if (ed < 897u) return 0.0f;
+  if (ed > 1150u) return 3.4028234663852886e38f;
+  return __uint_as_float((unsigned int)((mag >> 29) - (896ull << 23)));
+}
+
+// x = |v| 2^e split into q = rint(x) (round half to even; |q| <= 2048 by the
+// choice of e) and the remainder r = x - q, from A = floor(x 2^32): the
+// integer part and the 32 bits below it of the 53-bit mantissa.  r is exact
+// to 2^-31 absolute, far below what the FP16 residual slices keep (R1 rounds
+// r to 11 bits, R2 the rest to 11 more, ~2^-24 absolute).  The sign of v is
+// applied to both.
+__device__ __forceinline__ void split_int(unsigned long long b, int e, float &q, float &r) {
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  const int ed = (int)(mag >> 52);
+  const int sh = 1075 - 32 - ed - e;  // A = M >> sh, M the mantissa with its leading 1
+  unsigned long long A = 0;
+  if (ed != 0 && sh < 64) {
+    const unsigned long long M = (mag & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    A = sh >= 0 ? (M >> sh) : (M << (-sh));
+  }
+  const unsigned long long qi = (A + 0x7FFFFFFFull + ((A >> 32) & 1ull)) >> 32;
+  const long long fr = (long long)A - (long long)(qi << 32);  // in [-2^31, 2^31]
+  float qf = (float)(unsigned int)qi;
+  float rf = (float)(int)(fr >> 1) * 4.656612873077393e-10f;  // 2^-31
+  if (b >> 63) {
+    qf = -qf;
+    rf = -rf;
+  }
+  q = qf;
+  r = rf;
+}
+
+// Power-of-two scale exponent of a column from its largest magnitude (bits)
+// and its FP32 sum of squares: |C 2^e| <= 2047.5 and ||C 2^e||_2 below 2^12
+// with room for the rounding of NBA values.  FP64 arithmetic, which GB300
+// runs at a small fraction of its FP32 rate: one thread per column calls it.
+__device__ __forceinline__ int col_scale_exponent(unsigned long long mxb, float ss, int NBA) {
+  const double mx = __longlong_as_double((long long)mxb);
+  int e = 0;
+  if (mx > 0.0) {
+    // float truncation of the squares underestimates ||C||^2 by < 2^-21
+    // relative; the exact integer check of the caller keeps the exactness
+    const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
+    const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / nrm);
+    e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
+    e = max(-100, min(100, e));
+  }
+  return e;
+}
+
 // Slices of every fragment: slice plane s, fragment f, K chunk kc, column c
 // live at row (row_base_f + kc*ncol_f + c) of 64 FP16, i.e. one 2D-boxable
 // K-chunk-major layout shared by all fragments (one tensor map per batch).
-// grid.y = fragment, one warp per column.
-__global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, long long plane,
+// grid.y = fragment, one warp per column.  At most 40 registers a thread, so
+// that a 256-thread block fits in the registers a persistent energy kernel
+// leaves free on its SM: in a batch graph the next group's slicing runs
+// beside the current group's energy kernel.  (A single-pass form holding the
+// column in registers was measured slower: a 12 KB column took ~40 KB of
+// register file, leaving too few columns in flight per SM.)
+__global__ void __launch_bounds__(256, 6)
+    slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, long long plane,
                                    __half *__restrict__ slices, float *__restrict__ inv_scale,
                                    int col0, int col1, int vplane = 0,
                                    float *__restrict__ dcorr = nullptr) {
@@ -373,7 +412,7 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
       const unsigned long long mag =
           (unsigned long long)__double_as_longlong(v[u]) & 0x7FFFFFFFFFFFFFFFull;
       mxb = mag > mxb ? mag : mxb;
-      const float f = bits_to_float_trunc(mag, 0);
+      const float f = abs_trunc_f32(mag);
       ss = fmaf(f, f, ss);
     }
   }
@@ -383,16 +422,8 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
     mxb = other > mxb ? other : mxb;
     ss += __shfl_xor_sync(0xffffffffu, ss, o);
   }
-  const double mx = __longlong_as_double((long long)mxb);
-  int e = 0;
-  if (mx > 0.0) {
-    // float truncation of the squares underestimates ||C||^2 by < 2^-21
-    // relative; the exact integer check below keeps the exactness guarantee
-    const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
-    const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / nrm);
-    e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
-    e = max(-100, min(100, e));
-  }
+  int e = lane == 0 ? col_scale_exponent(mxb, ss, NBA) : 0;
+  e = __shfl_sync(0xffffffffu, e, 0);
   if (vplane && lane == 0) dcorr[F.col_base + col] = 0.0f;
   for (int attempt = 0; attempt < 64; ++attempt) {
     long long n2 = 0;  // sum of S0^2 (integers; <= 2^24 is the test)
@@ -407,15 +438,13 @@ __global__ void slice_batch_kernel(const FragDesc *__restrict__ fr, int nsl, lon
         if (k >= Kpad) break;
         __half h0 = hz, h1 = hz, h2 = hz, hv = hz;
         if (k < NBA) {
-          float xh, xl;
-          split_double(v[u], e, xh, xl);
-          const float q = rintf(xh);
-          const float r = (xh - q) + xl;  // xh - q exact
-          h0 = __float2half_rn(q);        // integer |q| <= 2048: exact in FP16
+          float q, r;
+          split_int((unsigned long long)__double_as_longlong(v[u]), e, q, r);
+          h0 = __float2half_rn(q);  // integer |q| <= 2048: exact in FP16
           h1 = __float2half_rn(r);
           h2 = __float2half_rn(r - __half2float(h1));
           const int qi = (int)q;
-          n2 += (long long)qi * qi;
+          n2 += qi * qi;  // |q| <= 2048: q^2 fits an int
           if (vplane) {
             // V = C*s in FP16; its rounding error against S0 + R1 is exact in FP32
             hv = __float2half_rn(q + r);
@@ -2037,6 +2066,36 @@ struct Group {
   DevBuf xbuf;          // 4-stage form: one 64 KB exchange tile per CTA
 };
 
+// Launch with the device's highest scheduling priority.  The persistent
+// energy kernels of a batch graph run beside the slicing of the next launch
+// group on a side branch; without priority the slicer's many small blocks,
+// ready at the same moment, fill the SMs first and the energy kernel's CTAs
+// wait for them to drain.  (The priority is recorded into graph nodes.)
+int energy_priority() {
+  static int prio = 1;
+  if (prio == 1) {
+    int least = 0, greatest = 0;
+    prio = cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess ? greatest : 0;
+  }
+  return prio;
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_hi(void (*k)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                      cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = energy_priority();
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Stage count of the paired kernel for a group.  The fourth 56 KB stage
 // (which needs the exchange tile transposed through global scratch instead of
 // shared memory) covers the cross-CTA refill round trip on long product
@@ -2060,12 +2119,17 @@ int pair_stages_for(const std::vector<FragDesc> &fh) {
 
 int launch_pair(const Group &g, PairParams Q, int npair, cudaStream_t s) {
   Q.xbuf = g.xbuf.as<float>();
+  cudaError_t e;
   if (g.pair_nstage == 4)
-    split_pair_kernel<4, true>
-        <<<2 * npair, NTHREADS, pair_smem_bytes(4, true), s>>>(g.tm, g.tmB, Q);
+    e = launch_hi(split_pair_kernel<4, true>, 2 * npair, NTHREADS, pair_smem_bytes(4, true), s,
+                  g.tm, g.tmB, Q);
   else
-    split_pair_kernel<3, false>
-        <<<2 * npair, NTHREADS, pair_smem_bytes(3, false), s>>>(g.tm, g.tmB, Q);
+    e = launch_hi(split_pair_kernel<3, false>, 2 * npair, NTHREADS, pair_smem_bytes(3, false),
+                  s, g.tm, g.tmB, Q);
+  if (e != cudaSuccess) {
+    set_error("paired energy kernel launch failed: %s", cudaGetErrorString(e));
+    return RIMP2_ERR_CUDA;
+  }
   return RIMP2_OK;
 }
 
@@ -2196,20 +2260,30 @@ int build_group(Group &g, cudaStream_t s) {
   return RIMP2_OK;
 }
 
-// Enqueue one evaluation of the group on s (graph-capturable: no sync, no alloc).
-int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null */) {
+// The group's inputs for its energy kernel: slices, scales, corrections and
+// orbital-energy pairs (graph-capturable: no sync, no alloc).
+int record_group_inputs(Group &g, cudaStream_t s) {
+  if (g.nfrag == 0) return RIMP2_OK;
+  const FragDesc *fr = g.frags.as<FragDesc>();
+  dim3 grid((unsigned)((g.max_ncol * 32LL + 255) / 256), (unsigned)g.nfrag);
+  slice_batch_kernel<<<grid, 256, 0, s>>>(fr, g.nsl, g.R * 64, g.slices.as<__half>(),
+                                          g.inv.as<float>(), 0, 0x7fffffff, g.pair ? 1 : 0,
+                                          g.dcorr.as<float>());
+  dim3 g2((unsigned)((g.max_nv + 255) / 256), (unsigned)g.nfrag);
+  eps_batch_kernel<<<g2, 256, 0, s>>>(fr, g.eo2.as<float2>(), g.ev2.as<float2>());
+  count_launch(2);
+  RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+// Enqueue one evaluation of the group on s (graph-capturable: no sync, no
+// alloc); with_inputs = false when its inputs were enqueued elsewhere.
+int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null */,
+                 bool with_inputs = true) {
   if (g.nfrag == 0) return RIMP2_OK;
   const FragDesc *fr = g.frags.as<FragDesc>();
   if (ev) RIMP2_CK(cudaEventRecord(ev[0], s));
-  {
-    dim3 grid((unsigned)((g.max_ncol * 32LL + 255) / 256), (unsigned)g.nfrag);
-    slice_batch_kernel<<<grid, 256, 0, s>>>(fr, g.nsl, g.R * 64, g.slices.as<__half>(),
-                                            g.inv.as<float>(), 0, 0x7fffffff, g.pair ? 1 : 0,
-                                            g.dcorr.as<float>());
-    dim3 g2((unsigned)((g.max_nv + 255) / 256), (unsigned)g.nfrag);
-    eps_batch_kernel<<<g2, 256, 0, s>>>(fr, g.eo2.as<float2>(), g.ev2.as<float2>());
-    count_launch(2);
-  }
+  if (with_inputs) RIMP2_TRY(record_group_inputs(g, s));
   RIMP2_CK(cudaMemsetAsync(g.queue.p, 0, sizeof(unsigned int), s));
   BatchParams P;
   P.frags = fr;
@@ -2246,10 +2320,10 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
     note_split_kernel(2);
   } else if (g.nsl == 2) {
     note_split_kernel(1);
-    split_batch_kernel<2, 3><<<grid, BATCH_THREADS, smem_bytes(2, 3), s>>>(g.tm, P);
+    RIMP2_CK(launch_hi(split_batch_kernel<2, 3>, grid, BATCH_THREADS, smem_bytes(2, 3), s, g.tm, P));
   } else {
     note_split_kernel(1);
-    split_batch_kernel<3, 2><<<grid, BATCH_THREADS, smem_bytes(3, 2), s>>>(g.tm, P);
+    RIMP2_CK(launch_hi(split_batch_kernel<3, 2>, grid, BATCH_THREADS, smem_bytes(3, 2), s, g.tm, P));
   }
   count_launch(1);
   if (ev) RIMP2_CK(cudaEventRecord(ev[2], s));
@@ -2471,7 +2545,7 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
         const unsigned long long mag =
             (unsigned long long)__double_as_longlong(v[q]) & 0x7FFFFFFFFFFFFFFFull;
         mxb = mag > mxb ? mag : mxb;
-        const float f = bits_to_float_trunc(mag, 0);
+        const float f = abs_trunc_f32(mag);
         ss = fmaf(f, f, ss);
       }
     }
@@ -2504,15 +2578,13 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
             const int nu = kc * 64 + q00 + 8 * hh + q;
             h0[q] = h1[q] = h2[q] = hz;
             if (live && nu < nbas) {
-              float xh, xl;
-              split_double(v[8 * hh + q], e, xh, xl);
-              const float qv = rintf(xh);
-              const float r = (xh - qv) + xl;
+              float qv, r;
+              split_int((unsigned long long)__double_as_longlong(v[8 * hh + q]), e, qv, r);
               h0[q] = __float2half_rn(qv);
               h1[q] = __float2half_rn(r);
               h2[q] = __float2half_rn(r - __half2float(h1[q]));
               const int qi = (int)qv;
-              n2 += (long long)qi * qi;
+              n2 += qi * qi;
             }
           }
           const int c = ((q00 >> 3) + hh) ^ sw;
@@ -2555,20 +2627,63 @@ struct SplitPlan {
   int nsm = 0;
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
+  // graph form of a plan with several launch groups: inputs on a side branch
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_in[3] = {nullptr, nullptr, nullptr};
   ~SplitPlan() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
+    for (auto &e : ev_in)
+      if (e) cudaEventDestroy(e);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (side) cudaStreamDestroy(side);
     plain_plan_destroy(plain);
   }
   int launches() const {
     int n = plain_plan_launches(plain);
     for (auto &x : g)
-      if (x.nfrag) n += 5;
+      if (x.nfrag) n += 5;  // slicing, eps, kernel, two reductions
     return n;
   }
 };
 
 bool split_supported() { return get_encode() != nullptr; }
+
+// Records the launch groups of a plan.  With two or more groups, every
+// group's inputs (slicing, orbital-energy pairs) go on a side branch, in the
+// order the energy kernels run, and each energy kernel waits only for its
+// own group's inputs: the slicing of the next group runs while the current
+// group's persistent kernel holds the SMs (a slicing block fits beside an
+// energy CTA), instead of between the two kernels.  The group with the least
+// slicing work goes first, since nothing hides its inputs.
+int record_plan_overlapped(SplitPlan *P, cudaStream_t s) {
+  int order[3], n = 0;
+  for (int k = 0; k < 3; ++k)
+    if (P->g[k].nfrag) order[n++] = k;
+  if (n < 2) {
+    for (int k = 0; k < n; ++k) RIMP2_TRY(record_group(P->g[order[k]], s, P->nsm, nullptr));
+    return RIMP2_OK;
+  }
+  int first = 0;
+  for (int k = 1; k < n; ++k)
+    if (P->g[order[k]].R < P->g[order[first]].R) first = k;  // R: 64-wide slice rows
+  std::swap(order[0], order[first]);
+  if (!P->side) {
+    set_error("internal: side stream of the plan not created");
+    return RIMP2_ERR_CUDA;
+  }
+  RIMP2_CK(cudaEventRecord(P->ev_fork, s));
+  RIMP2_CK(cudaStreamWaitEvent(P->side, P->ev_fork, 0));
+  for (int k = 0; k < n; ++k) {
+    RIMP2_TRY(record_group_inputs(P->g[order[k]], P->side));
+    RIMP2_CK(cudaEventRecord(P->ev_in[k], P->side));
+  }
+  for (int k = 0; k < n; ++k) {
+    RIMP2_CK(cudaStreamWaitEvent(s, P->ev_in[k], 0));
+    RIMP2_TRY(record_group(P->g[order[k]], s, P->nsm, nullptr, false));
+  }
+  return RIMP2_OK;
+}
 
 int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nvirt, const int *NBA,
                       const double *const *Ca, const double *const *eo, const double *const *ev,
@@ -2635,6 +2750,19 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
     }
   }
   if (graph) {
+    int ngroups = 0;
+    for (auto &g : P->g) ngroups += g.nfrag ? 1 : 0;
+    if (ngroups >= 2) {  // the side branch of record_plan_overlapped
+      if (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&P->ev_in[0], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&P->ev_in[1], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&P->ev_in[2], cudaEventDisableTiming) != cudaSuccess) {
+        set_error("stream/event creation for the batch graph failed");
+        delete P;
+        return RIMP2_ERR_CUDA;
+      }
+    }
     // the captured sequence needs the workspace already in place
     cudaError_t e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
@@ -2645,8 +2773,7 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
     }
     const long long n0 = rimp2_kernel_launch_count();
     int rc = plain_plan_record(P->plain, s);
-    for (auto &g : P->g)
-      if (rc == RIMP2_OK) rc = record_group(g, s, P->nsm, nullptr);
+    if (rc == RIMP2_OK) rc = record_plan_overlapped(P, s);
     e = cudaStreamEndCapture(s, &P->graph);
     // captured launches run at each graph launch, not here
     count_launch(-(int)(rimp2_kernel_launch_count() - n0));
@@ -2788,6 +2915,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
     slice_batch_kernel<<<(unsigned)(((long long)(col1 - col0) * 32 + 255) / 256), 256, 0, s>>>(
         fr, g.nsl, g.R * 64, g.slices.as<__half>(), g.inv.as<float>(), col0, col1,
         g.pair ? 1 : 0, g.dcorr.as<float>());
+    count_launch(1);
     e = cudaMemsetAsync(g.queue.p, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) {
       set_error("queue reset failed: %s", cudaGetErrorString(e));
@@ -2810,7 +2938,8 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
       Q.err = BP.err;
       const int npair = (int)std::min<long long>(Q.nitems - Q.item_begin, std::max(1, P->nsm / 2));
       note_split_kernel(2);
-      launch_pair(g, Q, npair, s);
+      rc = launch_pair(g, Q, npair, s);
+      if (rc != RIMP2_OK) break;
     } else {
       // pairs (i<=j) with j in [i0, i1): pair indices [i0(i0+1)/2, i1(i1+1)/2)
       const long long pb = (long long)i0 * (i0 + 1) / 2, pe = (long long)i1 * (i1 + 1) / 2;
@@ -2824,7 +2953,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
       else
         split_batch_kernel<3, 2><<<grid, BATCH_THREADS, smem_bytes(3, 2), s>>>(g.tm, BP);
     }
-    count_launch(2);
+    count_launch(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
       set_error("split launch failed: %s", cudaGetErrorString(e));
