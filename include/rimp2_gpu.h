@@ -316,13 +316,16 @@ int rimp2_calpha_from_ao(const int *NBA, const int *nbas, const int *nocc, const
 int rimp2_calpha_from_ao_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao,
                              const double *dV, const double *dCmo, double *dCalpha, void *stream);
 /* Same, with the AO->MO transform on the tcgen05 tensor cores (exact-integer
- * FP16 slices with two residual slices, ~2^-33 relative per product); the
- * metric Cholesky and the triangular solve stay FP64. */
+ * FP16 slices with two residual slices; Calpha within ~1e-8 of the FP64
+ * form); the metric Cholesky and the triangular solve stay FP64.  For
+ * nocc <= 80 its first half contracts over the middle AO index, relying on
+ * the (mu,nu) symmetry of ao stated above. */
 int rimp2_calpha_from_ao_split_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao,
                                    const double *dV, const double *dCmo, double *dCalpha,
                                    void *stream);
 /* Building blocks: the AO->MO transform alone, (alpha|a i) in the Calpha
- * layout (NBA,nvirt,nocc); split != 0 selects the tensor-core form. */
+ * layout (NBA,nvirt,nocc); split != 0 selects the tensor-core form (which,
+ * for nocc <= 80, uses the (mu,nu) symmetry of ao). */
 int rimp2_ao2mo_dev(int NBA, int nbas, int nocc, int nvirt, const double *dao, const double *dCmo,
                     double *dout, int split, void *stream);
 /* Lower Cholesky V = L L^T in place (n x n, strict upper

@@ -161,6 +161,10 @@ struct SlicedOp {
 // rows = columns of a column-major array: group g, row r at src + K*(r + nrows*g)
 int sliced_cols(SlicedOp &op, const double *src, int K, int nrows, int ngroups, int nsl,
                 cudaStream_t s);
+// half[i][alpha][mu] = sum_nu ao(alpha,mu,nu) Cmo(nu,i) in one fused pass over
+// the AO tensor; *handled = false when nocc is beyond the fused kernel
+int ao_half_fused(const double *ao, int NBA, int nbas, const double *Cmo, int nocc, double *half,
+                  cudaStream_t s, bool *handled);
 // rows m' = mu + nbas*alpha of (alpha|mu nu) over K = nu
 int sliced_ao(SlicedOp &op, const double *ao, int NBA, int nbas, int nsl, cudaStream_t s);
 // out[b*sOb + m*sOm + n*sOn] = sum_k A[a_row0 + b*a_bstride + m][k] * B[b_row0 + b*b_bstride + n][k]

@@ -339,7 +339,9 @@ int dev_ao2mo_split(int NBA, int nbas, int nocc, int nvirt, const double *ao, co
   const long long MK = (long long)NBA * nbas;
   DevBuf half;
   RIMP2_TRY(half.alloc(sizeof(double) * (size_t)MK * nocc, s));
-  {
+  bool fused = false;
+  RIMP2_TRY(ao_half_fused(ao, NBA, nbas, Cmo, nocc, half.as<double>(), s, &fused));
+  if (!fused) {
     SlicedOp Aao, Bocc;
     RIMP2_TRY(sliced_ao(Aao, ao, NBA, nbas, nsl, s));
     RIMP2_TRY(sliced_cols(Bocc, Cmo, nbas, nocc, 1, nsl, s));

@@ -2506,6 +2506,474 @@ __global__ void __launch_bounds__(192, 1)
   }
 }
 
+// ==========================================================================
+// Fused first half of the AO->MO transform on the tensor cores, one pass over
+// the FP64 AO tensor:  H[i][alpha][mu] = sum_nu (alpha|mu nu) Cmo(nu, i),
+// evaluated as sum_nu (alpha|nu mu) Cmo(nu, i): the three-centre integrals
+// are symmetric in their two AO indices, and the middle one is the short
+// stride (8 NBA bytes), so every 64-value chunk of a row lies in one memory
+// page (the last index is 8 NBA nbas bytes apart: a chunk would touch 64).
+// GEMM rows are (alpha, mu) -- 16 alpha x 8 mu per CTA tile, row r = a + 16 m
+// -- K = nu in chunks of 64, N = the occupied orbitals (NT <= 80, padded to
+// a multiple of 16).  The AO tensor is read once, by converter warps, with
+// coalesced loads (16 consecutive alpha of two mu rows per warp load), and
+// sliced in shared memory with a power-of-two scale per (row, K chunk):
+// |x 2^e| <= 511.5, so S0 is a 10-bit integer, and with the occupied MO
+// block sliced the same way (per column and chunk, precomputed) every
+// partial sum of S0a S0b over a chunk is below 64 * 511^2 < 2^24: the integer
+// part of each chunk's product is exact in FP32.  Products per element pair:
+// S0 S0 (L0), S0 R1 + R1 S0 + R1 R1 + S0 R2 + R2 S0 (L1).  Each chunk's L0/L1
+// go to one of two TMEM buffers; the epilogue scales them by the row and
+// column scales of that chunk (powers of two: exact) and adds them into a
+// double-float (FP32 hi + lo, two-sum) running total kept in TMEM, so the
+// result carries ~2^-40 of the chunk products' magnitude.  At the end of
+// the tile the totals are converted to FP64, staged in shared memory and
+// written as 64-byte runs of 8 mu per (i, alpha).
+// Roles: warps 0-15 converters (row r = 32 (w & 3) + lane, K quarter w >> 2
+// of each chunk: 16 values a thread), warp 16 MMA issuer and TMEM owner.
+// The converter warps are also the epilogue: each is bound to the TMEM lane
+// quadrant of its rows and takes a quarter of the NT columns; in iteration
+// c they slice chunk c and then fold chunk c-1's accumulators into the
+// running totals, while the tensor core runs chunk c.  Each thread copies
+// its 16 values of the next chunk into the FP64 slot (cp.async) once it has
+// handed the current chunk to the tensor core, and every thread prefetches
+// the chunk after that into L2.  Measured (clock64 per role, nbas=680): the
+// converter warps bound the kernel -- slicing and epilogue ~15k cycles per
+// 64-value chunk with four warps per scheduler, latency-bound at ~0.3
+// instructions per cycle -- while the copies wait ~100 cycles a chunk.
+// Every wait is bounded; on expiry
+// the CTA records an error code, drains its copies and MMAs and returns.
+// --------------------------------------------------------------------------
+constexpr int AH_TA = 16, AH_TM = 8;  // alpha x mu rows of a tile (16 x 8 = 128)
+constexpr int AH_CONV = 16;
+constexpr int AH_THREADS = 32 * (AH_CONV + 1);
+constexpr int AH_NT_MAX = 80;
+constexpr int AH_STG = AH_TA * 9;  // staged output doubles per column
+
+struct AoHalfParams {
+  const double *ao;   // (alpha|mu nu), alpha fastest: ao[alpha + NBA (mu + nbas nu)]
+  int NBA, nbas, nocc, NT, nks;
+  int ta_tiles;       // alpha tiles (of 16)
+  const float *sb;    // [chunk][NT] column scales of the sliced occupied MO block
+  double *half;       // H[i][alpha][mu]
+  uint32_t idesc;
+  int *err;
+};
+
+constexpr int ah_b_plane(int NT) { return NT * 128; }  // bytes of one B plane (NT rows x 64 FP16)
+constexpr int ah_stage_bytes(int NT) { return 3 * PANEL_BYTES + 3 * ah_b_plane(NT); }
+constexpr int AH_SLOT_BYTES = KSTEP * 128 * 8;  // one FP64 chunk of the tile (64 KB)
+constexpr int ah_smem_bytes(int NT) {
+  return 1024 + 2 * ah_stage_bytes(NT) + AH_SLOT_BYTES + 2 * 4 * 128 * 4 /*row max exchange*/ +
+         2 * 128 * 4 /*row scales*/ + 256 /*barriers, slot*/;
+}
+
+// 8-byte asynchronous global -> shared copy; src_bytes = 0 fills zeros and
+// reads nothing
+__device__ __forceinline__ void cp_async8_zfill(uint32_t dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const float (&v)[4]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3]))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// split_int with the integer part formed without an int->float conversion
+// (those run at a fraction of the FP32 rate): for 0 <= qi < 2^23 the float
+// with bits 0x4B000000 | qi is 2^23 + qi exactly, so subtracting 2^23 gives
+// qi.  Same results as split_int.
+__device__ __forceinline__ void split_int_fast(unsigned long long b, int e, float &q, float &r) {
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  const int ed = (int)(mag >> 52);
+  const int sh = 1075 - 32 - ed - e;
+  unsigned long long A = 0;
+  if (ed != 0 && sh < 64) {
+    const unsigned long long M = (mag & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    A = sh >= 0 ? (M >> sh) : (M << (-sh));
+  }
+  const unsigned long long qi = (A + 0x7FFFFFFFull + ((A >> 32) & 1ull)) >> 32;
+  const long long fr = (long long)A - (long long)(qi << 32);
+  const uint32_t sgn = (uint32_t)(b >> 63) << 31;
+  q = __uint_as_float(__float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)qi) - 8388608.0f) | sgn);
+  r = __uint_as_float(__float_as_uint((float)(int)(fr >> 1) * 4.656612873077393e-10f) ^ sgn);
+}
+
+// Exponent e with |x| 2^e <= 511.5 (to within 2^-11) for the largest
+// magnitude of a row or column chunk, from key = the top 32 bits of its FP64
+// pattern (11 exponent, 20 fraction bits): mx = m 2^E with m in [1, 2), and
+// m <= 1.998046875 (fraction key <= 0xFFE00) allows e = 8 - E.  A value that
+// shares the key but has nonzero lower bits gives |x| 2^e < 511.5003, which
+// rounds to |q| <= 512: still exact in FP16, and 64 products of two such
+// integers stay <= 2^24, exact in FP32.  At most 126, so that 2^-e is a
+// normal float; at least -126 (|x| < 2^134); 0 for a chunk of zeros and
+// subnormals.
+__device__ __forceinline__ int chunk_exponent_511(uint32_t key) {
+  const int ed = (int)(key >> 20);
+  if (ed == 0) return 0;
+  const int E = ed - 1023;
+  const int e = ((key & 0xFFFFFu) <= 0xFFE00u ? 8 : 7) - E;
+  return max(-126, min(126, e));
+}
+
+// Bounded vote over the converter threads (named barrier 2).
+__device__ __forceinline__ bool conv_any(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, o;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred o, 2, %2, q;\n\t"
+      "selp.u32 %0, 1, 0, o;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(32 * AH_CONV)
+      : "memory");
+  return r != 0;
+}
+
+__global__ void __maxnreg__(96)
+    ao_half_kernel(const __grid_constant__ CUtensorMap tmB, AoHalfParams P) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int NT = P.NT;
+  const int BPL = ah_b_plane(NT);
+  const int STAGE = 3 * PANEL_BYTES + 3 * BPL;
+  uint8_t *stages = base;
+  double *slot = (double *)(base + 2 * STAGE);                     // [64 k][128 rows] FP64
+  uint32_t *smx = (uint32_t *)(base + 2 * STAGE + AH_SLOT_BYTES);  // [2 parity][4 quarter][128]
+  float *sscale = (float *)(smx + 2 * 4 * 128);                    // [2][128]
+  uint64_t *bars = (uint64_t *)(sscale + 2 * 128);
+  // bars: stage_full[2], stage_empty[2], acc_full[2], acc_empty[2], drain
+  uint32_t *tmem_slot = (uint32_t *)(bars + 9);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+  const uint32_t sfull0 = smem_u32(&bars[0]), sempty0 = smem_u32(&bars[2]);
+  const uint32_t afull0 = smem_u32(&bars[4]), aempty0 = smem_u32(&bars[6]);
+  const uint32_t drain = smem_u32(&bars[8]);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ta = blockIdx.x % P.ta_tiles, tm = blockIdx.x / P.ta_tiles;
+  const int alpha0 = ta * AH_TA, mu0 = tm * AH_TM;
+  const int nks = P.nks;
+
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(sfull0 + 8 * b, 32 * AH_CONV);  // every converter thread (one with the B bytes)
+      mbar_init(sempty0 + 8 * b, 1);            // MMA commit
+      mbar_init(afull0 + 8 * b, 1);             // MMA commit
+      mbar_init(aempty0 + 8 * b, AH_CONV);      // converter warps, after reading the chunk
+    }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+  }
+  if (warp == AH_CONV) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                     smem_u32(tmem_slot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < AH_CONV) {
+    // ------------------------- converters and epilogue ------------------------
+    const int r = 32 * (warp & 3) + lane;  // tile row = TMEM lane of this thread
+    const int kq = warp >> 2;              // K quarter of each chunk; column quarter of N
+    const int a_l = r % AH_TA, m_l = r / AH_TA;
+    const int alpha = alpha0 + a_l, mu = mu0 + m_l;
+    const bool live = alpha < P.NBA && mu < P.nbas;
+    // row (alpha, mu) contracted over the middle index: (alpha|nu mu) =
+    // (alpha|mu nu), and the middle index is 8 NBA bytes apart, so a chunk of
+    // 64 values stays inside one memory page (the last index: 64 pages)
+    const long long kstride = P.NBA;
+    const double *src = P.ao + (live ? (long long)alpha + (long long)P.NBA * P.nbas * mu : 0);
+    const int within = r & 7;
+    int armed = -1;  // thread 0: parity of the last stage it armed for the B copy
+    int armed_b = 0;
+    // this thread's 16 values of a chunk in the FP64 slot: k = 16 kq + j
+    double *myslot = slot + (16 * kq) * 128 + r;
+    const uint32_t myslot_s = smem_u32(myslot);
+    // L2 prefetch of a later chunk: thread t covers the 16-alpha run (128
+    // bytes, at most two lines) of k = t / 8 and mu = mu0 + t % 8, so that
+    // the chunk's cp.async copies find their data in L2; with one chunk in
+    // flight per CTA the copies would otherwise wait out the slowest DRAM
+    // access of each chunk
+    const int pf_k = threadIdx.x >> 3, pf_m = mu0 + (threadIdx.x & 7);
+    const int pf_a = min(AH_TA, P.NBA - alpha0);  // alpha values of the tile
+    auto prefetch_chunk = [&](int c) {
+      const int k = c * KSTEP + pf_k;
+      if (k < P.nbas && pf_m < P.nbas) {
+        const double *p = P.ao + alpha0 + (long long)P.NBA * k + (long long)P.NBA * P.nbas * pf_m;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(p + (pf_a - 1)));
+      }
+    };
+    auto issue_chunk = [&](int c) {
+      const int k0 = c * KSTEP + 16 * kq;
+      const int lim = live ? min(16, P.nbas - k0) : 0;  // values that exist
+      const double *p = src + kstride * k0;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        cp_async8_zfill(myslot_s + j * 128 * 8, j < lim ? (const void *)p : (const void *)P.ao,
+                        j < lim ? 8u : 0u);
+        p += kstride;
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    // epilogue of chunk ce: its L0/L1 scaled by the row and column scales of
+    // the chunk and added to the running double-float totals (TMEM), or on
+    // the last chunk turned into FP64 in the staging area
+    const int ncol = NT / 4, col0 = kq * ncol;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+    const uint32_t rs_hi = tmem + lane_off + (uint32_t)(4 * NT);
+    const uint32_t rs_lo = rs_hi + (uint32_t)NT;
+    auto epilogue = [&](int ce) -> bool {
+      const int b = ce & 1;
+      if (!mbar_wait(afull0 + 8 * b, (uint32_t)((ce >> 1) & 1), abort_flag, P.err, 25)) return false;
+      tc_fence_after();
+      const float sa = sscale[b * 128 + r];
+      const uint32_t tL0 = tmem + lane_off + (uint32_t)(b * 2 * NT);
+      const float *sbc = P.sb + (size_t)ce * NT;
+      const bool last = ce + 1 == nks;
+      double *stg = reinterpret_cast<double *>(stages);
+      for (int col = col0; col < col0 + ncol; col += 4) {
+        float l0[4], l1[4], hi[4], lo[4];
+        tmem_ld4(tL0 + col, l0);
+        tmem_ld4(tL0 + NT + col, l1);
+        if (ce > 0) {
+          tmem_ld4(rs_hi + col, hi);
+          tmem_ld4(rs_lo + col, lo);
+        }
+        tmem_wait_ld();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float sc = sa * sbc[col + k];  // power of two: the products below are exact
+          const float xh = l0[k] * sc, xl = l1[k] * sc;
+          if (ce == 0) {
+            hi[k] = xh;
+            lo[k] = xl;
+          } else {  // two-sum of the high parts, low parts added
+            const float s = hi[k] + xh;
+            const float bv = s - hi[k];
+            const float err = (hi[k] - (s - bv)) + (xh - bv);
+            lo[k] = lo[k] + xl + err;
+            hi[k] = s;
+          }
+        }
+        if (!last) {
+          tmem_st4(rs_hi + col, hi);
+          tmem_st4(rs_lo + col, lo);
+        } else {
+          // [column][alpha][mu] with a 9-double pitch per alpha
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            stg[(col + k) * AH_STG + a_l * 9 + m_l] = (double)hi[k] + (double)lo[k];
+        }
+      }
+      if (!last) tmem_wait_st();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(aempty0 + 8 * b);
+      return true;
+    };
+    bool ok_all = true;
+    if (nks > 1) prefetch_chunk(1);
+    issue_chunk(0);
+    for (int c = 0; c < nks; ++c) {
+      if (c + 2 < nks) prefetch_chunk(c + 2);
+      const int b = c & 1;
+      // chunk c has landed (each thread reads only the values it copied)
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      double v[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = myslot[j * 128];
+      uint32_t key = 0;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const uint32_t kj = (uint32_t)(((unsigned long long)__double_as_longlong(v[j]) >> 32) &
+                                       0x7FFFFFFFu);
+        key = kj > key ? kj : key;
+      }
+      smx[(b * 4 + kq) * 128 + r] = key;
+      bool ok = true;
+      if (c >= 2) ok = mbar_wait(sempty0 + 8 * b, (uint32_t)(((c - 2) >> 1) & 1), abort_flag, P.err, 21);
+      if (conv_any(!ok)) {  // also the barrier of the max exchange
+        ok_all = false;
+        break;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t o = smx[(b * 4 + q) * 128 + r];
+        key = o > key ? o : key;
+      }
+      const int e = chunk_exponent_511(key);
+      if (kq == 0) sscale[b * 128 + r] = ldexpf(1.0f, -e);
+      uint8_t *st = stages + b * STAGE;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        __align__(16) __half2 h0[4], h1[4], h2[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {  // two values at a time, packed conversions
+          float qa, ra, qb, rb;
+          split_int_fast((unsigned long long)__double_as_longlong(v[8 * g + 2 * q]), e, qa, ra);
+          split_int_fast((unsigned long long)__double_as_longlong(v[8 * g + 2 * q + 1]), e, qb, rb);
+          h0[q] = __floats2half2_rn(qa, qb);  // |q| <= 512: exact in FP16
+          h1[q] = __floats2half2_rn(ra, rb);
+          const float2 f1 = __half22float2(h1[q]);
+          h2[q] = __floats2half2_rn(ra - f1.x, rb - f1.y);
+        }
+        const int phys = (2 * kq + g) ^ within;  // 128-byte swizzle of 16-byte chunks
+        const int off = (r >> 3) * 1024 + within * 128 + phys * 16;
+        *reinterpret_cast<uint4 *>(st + 0 * PANEL_BYTES + off) = *reinterpret_cast<const uint4 *>(h0);
+        *reinterpret_cast<uint4 *>(st + 1 * PANEL_BYTES + off) = *reinterpret_cast<const uint4 *>(h1);
+        *reinterpret_cast<uint4 *>(st + 2 * PANEL_BYTES + off) = *reinterpret_cast<const uint4 *>(h2);
+      }
+      // generic-proxy writes of the A panels become visible to the tensor core
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (threadIdx.x == 0) {
+        const uint32_t fb = sfull0 + 8 * b;
+        mbar_expect_tx(fb, 3 * BPL);
+        armed = (int)((c >> 1) & 1);
+        armed_b = b;
+        const uint32_t dst = smem_u32(st + 3 * PANEL_BYTES);
+#pragma unroll
+        for (int p = 0; p < 3; ++p) tma_load_3d(dst + p * BPL, &tmB, fb, 0, 0, 3 * c + p);
+      } else {
+        mbar_arrive(sfull0 + 8 * b);
+      }
+      // the next chunk's copies overlap the previous chunk's epilogue and
+      // the next iteration's start (the L2 prefetch keeps their latency short)
+      if (c + 1 < nks) issue_chunk(c + 1);
+      // the previous chunk's epilogue runs while this chunk's MMAs do
+      if (c >= 1 && conv_any(!epilogue(c - 1))) {
+        ok_all = false;
+        break;
+      }
+    }
+    // copies still in flight land before the CTA may exit
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (ok_all && conv_any(!epilogue(nks - 1))) ok_all = false;
+    if (ok_all) {
+      asm volatile("bar.sync 2, %0;" ::"r"(32 * AH_CONV) : "memory");
+      const double *stg = reinterpret_cast<const double *>(stages);
+      for (int idx = threadIdx.x; idx < P.nocc * AH_TA * AH_TM; idx += 32 * AH_CONV) {
+        const int ml = idx & 7, al = (idx >> 3) & 15, n = idx >> 7;
+        const int ga = alpha0 + al, gm = mu0 + ml;
+        if (ga < P.NBA && gm < P.nbas)
+          P.half[((long long)n * P.NBA + ga) * P.nbas + gm] = stg[n * AH_STG + al * 9 + ml];
+      }
+    }
+    if (threadIdx.x == 0 && armed >= 0 && *abort_flag) {
+      // the last B copy completes before the CTA may exit
+      const long long t0 = clock64();
+      while (!mbar_test(sfull0 + 8 * armed_b, (uint32_t)armed) && clock64() - t0 < WAIT_BUDGET) {
+      }
+    }
+  } else if (warp == AH_CONV) {
+    // ------------------------------ MMA issuer -------------------------------
+    if (lane == 0) {
+      for (int c = 0; c < nks; ++c) {
+        const int b = c & 1;
+        if (!mbar_wait(sfull0 + 8 * b, (uint32_t)((c >> 1) & 1), abort_flag, P.err, 23)) break;
+        if (c >= 2 &&
+            !mbar_wait(aempty0 + 8 * b, (uint32_t)(((c - 2) >> 1) & 1), abort_flag, P.err, 24))
+          break;
+        tc_fence_after();
+        const uint32_t sA = smem_u32(stages + b * STAGE);
+        const uint32_t sB = sA + 3 * PANEL_BYTES;
+        const uint32_t dL0 = tmem + (uint32_t)(b * 2 * NT);
+        const uint32_t dL1 = dL0 + (uint32_t)NT;
+#pragma unroll
+        for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
+          const uint32_t koff = k16 * 32;
+          const uint64_t a0 = smem_desc(sA + koff), a1 = smem_desc(sA + PANEL_BYTES + koff);
+          const uint64_t a2 = smem_desc(sA + 2 * PANEL_BYTES + koff);
+          const uint64_t b0 = smem_desc(sB + koff), b1 = smem_desc(sB + BPL + koff);
+          const uint64_t b2 = smem_desc(sB + 2 * BPL + koff);
+          const uint32_t acc = k16 > 0 ? 1u : 0u;  // each chunk starts its own sums
+          mma_f16_id(dL0, a0, b0, P.idesc, acc);
+          mma_f16_id(dL1, a0, b1, P.idesc, acc);
+          mma_f16_id(dL1, a1, b0, P.idesc, 1u);
+          mma_f16_id(dL1, a1, b1, P.idesc, 1u);
+          mma_f16_id(dL1, a0, b2, P.idesc, 1u);
+          mma_f16_id(dL1, a2, b0, P.idesc, 1u);
+        }
+        mma_commit(sempty0 + 8 * b);  // the stage may be refilled
+        mma_commit(afull0 + 8 * b);   // the chunk's products are in TMEM
+      }
+      mma_commit(drain);
+      const long long t0 = clock64();
+      while (!mbar_test(drain, 0) && clock64() - t0 < WAIT_BUDGET) {
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == AH_CONV) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
+// Occupied MO block sliced for ao_half_kernel: column n (orbital), chunk c of
+// 64 nu values, scale per (column, chunk) with |x 2^e| <= 511.5; planes S0,
+// R1, R2 at Bsl[(3 c + p) NT + n][64] (plain rows; the TMA copy swizzles
+// them), scale 2^-e at sb[c NT + n].  One warp per (column, chunk); columns
+// n >= nocc and nu >= nbas are zero.
+__global__ void ao_occ_slice_kernel(const double *__restrict__ Cmo, int nbas, int nocc, int NT,
+                                    int nks, __half *__restrict__ Bsl, float *__restrict__ sb) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= NT * nks) return;
+  const int n = w % NT, c = w / NT;
+  double v[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int nu = c * KSTEP + lane + 32 * q;
+    v[q] = (n < nocc && nu < nbas) ? Cmo[(size_t)n * nbas + nu] : 0.0;
+  }
+  uint32_t key = 0;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const uint32_t kq =
+        (uint32_t)(((unsigned long long)__double_as_longlong(v[q]) >> 32) & 0x7FFFFFFFu);
+    key = kq > key ? kq : key;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint32_t other = __shfl_xor_sync(0xffffffffu, key, o);
+    key = other > key ? other : key;
+  }
+  const int e = chunk_exponent_511(key);
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    float qv, rv;
+    split_int((unsigned long long)__double_as_longlong(v[q]), e, qv, rv);
+    const __half h1 = __float2half_rn(rv);
+    const size_t k = lane + 32 * q;
+    Bsl[((size_t)(3 * c + 0) * NT + n) * 64 + k] = __float2half_rn(qv);
+    Bsl[((size_t)(3 * c + 1) * NT + n) * 64 + k] = h1;
+    Bsl[((size_t)(3 * c + 2) * NT + n) * 64 + k] = __float2half_rn(rv - __half2float(h1));
+  }
+  if (lane == 0) sb[(size_t)c * NT + n] = ldexpf(1.0f, -e);
+}
+
 // AO tensor rows: row m' = mu + nbas*alpha of (alpha|mu nu) over K = nu.
 // One CTA owns 32 alpha x 8 mu rows, one thread per row, warps alpha-fastest
 // so every load of a nu-step is one 256-byte segment.  Same scale rule and
@@ -3114,6 +3582,71 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
   }
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
+  return RIMP2_OK;
+}
+
+// First half of the AO->MO transform, fused (ao_half_kernel): the occupied MO
+// block is sliced per (column, 64-wide nu chunk), then one pass over the AO
+// tensor forms half[i][alpha][mu].  *handled = false (nothing launched) when
+// nocc exceeds the kernel's 80 columns; the caller then takes the sliced path.
+int ao_half_fused(const double *ao, int NBA, int nbas, const double *Cmo, int nocc, double *half,
+                  cudaStream_t s, bool *handled) {
+  *handled = false;
+  const int NT = (nocc + 15) / 16 * 16;
+  if (NT > AH_NT_MAX || nocc <= 0) return RIMP2_OK;
+  auto encode = get_encode();
+  if (!encode) {
+    set_error("cuTensorMapEncodeTiled entry point unavailable");
+    return RIMP2_ERR_UNSUPPORTED;
+  }
+  const int nks = (nbas + KSTEP - 1) / KSTEP;
+  const long long ntiles = (long long)((NBA + AH_TA - 1) / AH_TA) * ((nbas + AH_TM - 1) / AH_TM);
+  if (ntiles > 2147483647LL) {
+    set_error("AO transform too large for one launch (%lld tiles)", ntiles);
+    return RIMP2_ERR_ARG;
+  }
+  DevBuf Bsl, sb;
+  RIMP2_TRY(Bsl.alloc(sizeof(__half) * (size_t)3 * nks * NT * 64, s));
+  RIMP2_TRY(sb.alloc(sizeof(float) * (size_t)nks * NT, s));
+  const long long nw = (long long)NT * nks;
+  ao_occ_slice_kernel<<<(unsigned)((nw * 32 + 255) / 256), 256, 0, s>>>(
+      Cmo, nbas, nocc, NT, nks, Bsl.as<__half>(), sb.as<float>());
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  CUtensorMap tm;
+  cuuint64_t dims[3] = {64, (cuuint64_t)NT, (cuuint64_t)(3 * nks)};
+  cuuint64_t strides[2] = {128, (cuuint64_t)NT * 128};
+  cuuint32_t box[3] = {KSTEP, (cuuint32_t)NT, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult cr = encode(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, Bsl.p, dims, strides, box, estr,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
+    return RIMP2_ERR_CUDA;
+  }
+  AoHalfParams P;
+  P.ao = ao;
+  P.NBA = NBA;
+  P.nbas = nbas;
+  P.nocc = nocc;
+  P.NT = NT;
+  P.nks = nks;
+  P.ta_tiles = (NBA + AH_TA - 1) / AH_TA;
+  P.sb = sb.as<float>();
+  P.half = half;
+  P.idesc = (1u << 4) | ((uint32_t)(NT >> 3) << 17) | ((uint32_t)(TILE >> 4) << 24);
+  P.err = device_error_word();
+  const int smem = ah_smem_bytes(NT);
+  RIMP2_CK(cudaFuncSetAttribute(ao_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int resident = 0;
+  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, ao_half_kernel, AH_THREADS,
+                                                         smem));
+  if (resident < 1) return RIMP2_OK;  // cannot be resident here: the sliced path runs
+  ao_half_kernel<<<(unsigned)ntiles, AH_THREADS, smem, s>>>(tm, P);
+  count_launch(1);
+  RIMP2_CK(cudaGetLastError());
+  *handled = true;
   return RIMP2_OK;
 }
 

@@ -116,3 +116,33 @@ def test_split_ao2mo_matches_fp64(NBA, nbas, nocc):
     Ep, E = api.energy(nvirt, nocc, NBA, Casp, eo, ev, precision=api.PREC_SPLIT)
     assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= 1e-7
     assert abs(E - Er) <= 1e-7 * abs(Er)
+
+
+@pytest.mark.parametrize("NBA,nbas,nocc", [(75, 37, 4), (200, 130, 13), (130, 201, 80),
+                                           (96, 70, 7), (180, 230, 85)])
+def test_split_ao2mo_transform_vs_fp64(NBA, nbas, nocc):
+    """The AO->MO transform alone, tensor-core form against the FP64 form on
+    the same inputs, within 1e-8 of the largest element (measured 1.4-5.9e-9,
+    the fused first half and the sliced one alike): odd NBA (rows not
+    16-byte aligned), nbas not a multiple of the 8-row mu tile nor of the
+    64-wide K chunk, 16 to 80 occupied columns in the fused first half, and
+    nocc = 85 beyond it (the sliced first half)."""
+    import torch
+    from rimp2_gpu_gb300 import api
+    nvirt = nbas - nocc
+    dao = torch.zeros(NBA * nbas * nbas, dtype=torch.float64, device="cuda")
+    dV = torch.zeros(NBA * NBA, dtype=torch.float64, device="cuda")
+    api.gen_ao_dev(13, NBA, nbas, dao.data_ptr(), dV.data_ptr())
+    dC = t(O.gen_mo(13, nbas))
+    o64 = torch.zeros(NBA * nvirt * nocc, dtype=torch.float64, device="cuda")
+    osp = torch.zeros_like(o64)
+    api.ao2mo_dev(NBA, nbas, nocc, nvirt, dao.data_ptr(), dC.data_ptr(), o64.data_ptr(),
+                  split=False)
+    api.ao2mo_dev(NBA, nbas, nocc, nvirt, dao.data_ptr(), dC.data_ptr(), osp.data_ptr(),
+                  split=True)
+    torch.cuda.synchronize()
+    api.sync_status()
+    a, b = osp.cpu().numpy(), o64.cpu().numpy()
+    err = np.abs(a - b).max() / np.abs(b).max()
+    print(f"\nsplit AO->MO NBA={NBA} nbas={nbas} nocc={nocc}: {err:.2e} of the largest element")
+    assert err <= 1e-8
