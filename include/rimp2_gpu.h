@@ -74,10 +74,10 @@ int rimp2_last_timing(float *ms4);
 /* Energy kernel of the last split-form launch: 0 none yet, 1 one-CTA tile
  * kernel (128x128 MMA), 2 paired-CTA kernel (cta_group::2, 256x128 MMA over
  * two occupied pairs, three products per element pair with a per-column
- * diagonal correction).  One-residual-slice fragments with nocc >= 10 and
- * NBA >= 1024 use the paired kernel (shorter auxiliary spaces run faster on
- * the one-CTA kernel); RIMP2_PAIR_KERNEL=0 or =1 in the environment
- * overrides that choice. */
+ * diagonal correction).  One-residual-slice fragments use the kernel the
+ * shape-bucket kernel table picks (rimp2_set_split_kernel_rule: the paired
+ * kernel for enough occupied orbitals and a long enough auxiliary space);
+ * RIMP2_PAIR_KERNEL=0 or =1 in the environment overrides that choice. */
 int rimp2_last_split_kernel(void);
 /* Measured FP64 tensor-op (DMMA) throughput of this GPU in TFLOP/s, the
  * denominator for the plain kernel's roofline fraction: independent DMMA
@@ -268,8 +268,8 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
 
 /* Batched energies of many fragments of uneven size, all resident on the
  * device, in ONE persistent launch per kernel group (one residual slice on
- * the paired-CTA kernel -- nocc >= 10 and NBA >= 1024 -- or on the one-CTA
- * kernel, two residual slices, plain FP64): a device-side queue of
+ * the paired-CTA kernel or on the one-CTA kernel, per the kernel table of
+ * rimp2_set_split_kernel_rule; two residual slices; plain FP64): a device-side queue of
  * (fragment, pair, tile pair) work items ordered heaviest fragment first,
  * drained by one CTA (pair of CTAs) per SM (pair of SMs).  nslices[f] = 1 or 2 runs
  * fragment f in the split form with that many residual slices; 0 runs it in
@@ -294,6 +294,17 @@ int rimp2_batch_plan_destroy(void *plan);
  * pair energy has too few (a,b) terms to average the split form's error).
  * Every split-precision entry point follows the table. */
 int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices);
+/* Energy-kernel table of the one-residual-slice split form: fragments with
+ * nvirt >= nvirt_min[k] (largest such k) run the paired-CTA kernel (256-row
+ * tiles on a pair of SMs, three FP16 products per element pair) when nocc >=
+ * min_nocc[k] and NBA >= min_nba[k], else the one-CTA kernel (128-row tiles,
+ * four products).  Default: the autotuner's measured thresholds.  The
+ * environment variable RIMP2_PAIR_KERNEL=0 or =1 overrides the table. */
+int rimp2_set_split_kernel_rule(int n, const int *nvirt_min, const int *min_nocc,
+                                const int *min_nba);
+/* Energy kernel a fragment of this shape runs in the split form with the
+ * current tables: 0 FP64 tier, 1 one-CTA kernel, 2 paired-CTA kernel. */
+int rimp2_split_kernel_for(int nvirt, int nocc, int NBA);
 
 /* ---- synthetic fragments (benchmark / test inputs; no counterpart in the
  * reference, whose fixtures are constants written by generate.F90) --------

@@ -70,6 +70,8 @@ SIGNATURES = {
     "rimp2_batch_plan_execute": ([_vp, _vp], C.c_int),
     "rimp2_batch_plan_destroy": ([_vp], C.c_int),
     "rimp2_set_split_buckets": ([C.c_int, _ip, _ip], C.c_int),
+    "rimp2_set_split_kernel_rule": ([C.c_int, _ip, _ip, _ip], C.c_int),
+    "rimp2_split_kernel_for": ([C.c_int, C.c_int, C.c_int], C.c_int),
     "rimp2_calpha_from_ao": ([_ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp], C.c_int),
     "rimp2_calpha_from_ao_dev": ([C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp],
                                  C.c_int),

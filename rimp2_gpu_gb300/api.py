@@ -332,6 +332,19 @@ def split_nslices(nvirt, nocc, NBA):
     return lib().rimp2_split_nslices(nvirt, nocc, NBA)
 
 
+def set_split_kernel_rule(nvirt_min, min_nocc, min_nba):
+    """Install the energy-kernel table of the one-residual-slice split form
+    (paired-CTA kernel where nocc >= min_nocc and NBA >= min_nba)."""
+    n = len(nvirt_min)
+    call("rimp2_set_split_kernel_rule", n, (C.c_int * n)(*nvirt_min), (C.c_int * n)(*min_nocc),
+         (C.c_int * n)(*min_nba))
+
+
+def split_kernel_for(nvirt, nocc, NBA):
+    """0 FP64 tier, 1 one-CTA kernel, 2 paired-CTA kernel for this shape."""
+    return int(lib().rimp2_split_kernel_for(nvirt, nocc, NBA))
+
+
 def calpha_from_ao(NBA, nbas, nocc, nvirt, ao, V, Cmo):
     """Calpha(NBA,nvirt,nocc) from AO three-centre integrals, metric and MO
     coefficients (FP64 Cholesky + triangular solve on the GPU)."""

@@ -7,8 +7,21 @@ GPU three ways -- the plain FP64 kernel (the reference values) and the split
 kernel with one and with two residual slices -- and picks the cheapest slice
 count whose worst pair-energy relative error over the sample stays below
 half of the 1e-7 target (a 2x margin for fragments not in the sample).  It
-also records the split kernel's time per bucket.  The table is installed in
-the library with ``apply`` (rimp2_set_split_buckets) and can be saved as
+also records the split kernel's time per bucket.
+
+For every bucket that runs one residual slice it then picks the energy
+kernel, i.e. the tile shape: the one-CTA kernel (128 x 128 tiles, four
+products per element pair) or the paired-CTA kernel (256 x 128 tiles on a
+pair of SMs sharing the B operand, three products, a dummy CTA when an
+occupied index has no partner).  It times both on a grid of occupied
+counts and auxiliary sizes at the bucket's middle virtual count, each shape
+replicated in one graph-launched batch plan until the launch does about
+2 ms of work (CUDA events, best of three), and keeps the thresholds
+(paired kernel where nocc >= min_nocc and NBA >= min_nba) that minimise the
+summed time over the grid.
+
+The tables are installed in the library with ``apply``
+(rimp2_set_split_buckets, rimp2_set_split_kernel_rule) and can be saved as
 JSON.  Every number it uses is measured on the GPU it runs on.
 
     python -m rimp2_gpu_gb300.autotune --out rimp2_gpu_gb300/tuning/split_buckets.json
@@ -79,6 +92,102 @@ def _run(nocc, nvirt, NBA, seed):
     return res
 
 
+KGRID_NOCC = [4, 8, 12, 16, 32]
+KGRID_NBA = [256, 512, 1024, 2048, 4096]
+NEVER = 1 << 30  # a threshold no fragment reaches
+KWORK = 2.0e12   # effective FLOP per timed launch (about 2 ms of work)
+
+
+def _time_kernels(nocc, nvirt, NBA, seed):
+    """Milliseconds per graph launch of a batch of `copies` fragments of one
+    shape (one residual slice), one-CTA and paired kernel."""
+    import torch
+    eff = 2.0 * NBA * (nocc * nvirt) ** 2
+    copies = int(max(1, min(64, round(KWORK / eff))))
+    st = torch.cuda.Stream()
+    s = st.cuda_stream
+    with torch.cuda.stream(st):
+        dC = torch.empty(NBA * nvirt * nocc, dtype=torch.float64, device="cuda")
+        deo = torch.empty(nocc, dtype=torch.float64, device="cuda")
+        dev = torch.empty(nvirt, dtype=torch.float64, device="cuda")
+        outs = [(torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda"),
+                 torch.zeros(1, dtype=torch.float64, device="cuda")) for _ in range(copies)]
+    api.gen_fragment_dev(seed, nocc, nvirt, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(),
+                         stream=s)
+    frags = [(nocc, nvirt, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(), E.data_ptr(),
+              T.data_ptr()) for E, T in outs]
+    res = {}
+    old = os.environ.get("RIMP2_PAIR_KERNEL")
+    try:
+        for kern, name in (("0", "one"), ("1", "pair")):
+            os.environ["RIMP2_PAIR_KERNEL"] = kern
+            plan = api.BatchPlan(frags, nslices=[1] * copies, graph=True, stream=s)
+            plan.execute(stream=s)
+            best = float("inf")
+            for _ in range(3):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                plan.execute(stream=s)
+                e1.record(st)
+                st.synchronize()
+                best = min(best, e0.elapsed_time(e1))
+            api.sync_status(s)
+            plan.close()
+            res[name] = best
+    finally:
+        if old is None:
+            os.environ.pop("RIMP2_PAIR_KERNEL", None)
+        else:
+            os.environ["RIMP2_PAIR_KERNEL"] = old
+    res["copies"] = copies
+    return res
+
+
+def _fit_rule(grid):
+    """Thresholds (min_nocc, min_nba) minimising the summed time of the grid
+    when the paired kernel runs exactly where nocc >= min_nocc and NBA >=
+    min_nba."""
+    cn = sorted({g["nocc"] for g in grid}) + [NEVER]
+    cb = sorted({g["NBA"] for g in grid}) + [NEVER]
+    best = None
+    for mo in cn:
+        for mb in cb:
+            t = sum(g["pair_ms"] if (g["nocc"] >= mo and g["NBA"] >= mb) else g["one_ms"]
+                    for g in grid)
+            if best is None or t < best[0] - 1e-9:
+                best = (t, mo, mb)
+    return best
+
+
+def tune_kernels(buckets, seed=91):
+    """Energy-kernel thresholds for the one-residual-slice buckets."""
+    rule = []
+    for k, b in enumerate(buckets):
+        if b["nslices"] != 1:
+            continue
+        lo = b["nvirt_min"]
+        hi = BUCKET_TOP[BUCKET_EDGES.index(lo)] if lo in BUCKET_EDGES else lo + 128
+        nv = (lo + hi) // 2
+        grid = []
+        for n, nocc in enumerate(KGRID_NOCC):
+            for m, NBA in enumerate(KGRID_NBA):
+                r = _time_kernels(nocc, nv, NBA, seed + 1000 * k + 10 * n + m)
+                grid.append({"nocc": nocc, "nvirt": nv, "NBA": NBA, "copies": r["copies"],
+                             "one_ms": r["one"], "pair_ms": r["pair"]})
+        t, mo, mb = _fit_rule(grid)
+        rule.append({"nvirt_min": lo, "min_nocc": mo, "min_nba": mb,
+                     "grid_ms_chosen": t,
+                     "grid_ms_one_only": sum(g["one_ms"] for g in grid),
+                     "grid_ms_pair_only": sum(g["pair_ms"] for g in grid), "grid": grid})
+    if rule:  # below the first one-slice bucket (an explicit nslices = 1)
+        first = dict(rule[0], nvirt_min=0)
+        first.pop("grid", None)
+        first["note"] = "thresholds of the first measured bucket"
+        rule.insert(0, first)
+    return rule
+
+
 def tune(seed=77):
     table = []
     for k, lo in enumerate(BUCKET_EDGES):
@@ -99,12 +208,17 @@ def tune(seed=77):
                      "FP32-accumulated correction against; the library also sends every "
                      "fragment with nocc*nvirt < 64 to FP64 (its FP32 epilogue rounding "
                      "leaves 2-5e-8 on such pair energies)"}
-    return {"target": TARGET, "margin": 0.5, "buckets": [fixed] + table}
+    return {"target": TARGET, "margin": 0.5, "buckets": [fixed] + table,
+            "kernel_rule": tune_kernels(table)}
 
 
 def apply(table):
     b = table["buckets"]
     api.set_split_buckets([x["nvirt_min"] for x in b], [x["nslices"] for x in b])
+    r = table.get("kernel_rule")
+    if r:
+        api.set_split_kernel_rule([x["nvirt_min"] for x in r], [x["min_nocc"] for x in r],
+                                  [x["min_nba"] for x in r])
 
 
 def load(path):
@@ -117,8 +231,15 @@ def load(path):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
+    ap.add_argument("--kernels-only", default=None, metavar="TABLE",
+                    help="keep the slice counts of this JSON table, re-measure the kernel rule")
     a = ap.parse_args()
-    t = tune()
+    if a.kernels_only:
+        with open(a.kernels_only) as f:
+            t = json.load(f)
+        t["kernel_rule"] = tune_kernels([x for x in t["buckets"] if x["nvirt_min"] > 0])
+    else:
+        t = tune()
     apply(t)
     txt = json.dumps(t, indent=1)
     if a.out:

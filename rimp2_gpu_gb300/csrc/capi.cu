@@ -997,6 +997,63 @@ int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices) {
   return RIMP2_OK;
 }
 
+// Energy kernel of one-residual-slice fragments by shape bucket: the paired-
+// CTA kernel (256-row tiles on an SM pair, three products per element pair)
+// when nocc >= min_nocc and NBA >= min_nba of the bucket (largest nvirt_min
+// <= nvirt), else the one-CTA kernel (128-row tiles, four products).  The
+// paired kernel's per-item costs (the exchange-tile transpose, cross-CTA
+// hand-offs, a dummy CTA for an odd count of i <= j) lose on short auxiliary
+// spaces and few occupied orbitals.  Default = the thresholds measured by
+// rimp2_gpu_gb300/autotune.py on GB300 (rimp2_gpu_gb300/tuning/
+// split_buckets.json, "kernel_rule"); rimp2_set_split_kernel_rule replaces it.
+struct KernelRule {
+  int nvirt_min, min_nocc, min_nba;
+};
+static std::vector<KernelRule> g_krule = {{0, 32, 1024}, {192, 32, 1024}, {256, 16, 2048},
+                                           {384, 16, 1024}};
+
+}  // extern "C"
+
+namespace rimp2 {
+bool pair_kernel_for(int nocc, int nvirt, int NBA) {
+  const char *e = getenv("RIMP2_PAIR_KERNEL");
+  if (e && e[0] == '0') return false;
+  if (e && e[0] == '1') return true;
+  std::lock_guard<std::mutex> lk(g_bucket_mu);
+  KernelRule r = g_krule.front();
+  for (auto &b : g_krule)
+    if (nvirt >= b.nvirt_min) r = b;
+  return nocc >= r.min_nocc && NBA >= r.min_nba;
+}
+}  // namespace rimp2
+
+extern "C" {
+
+int rimp2_set_split_kernel_rule(int n, const int *nvirt_min, const int *min_nocc,
+                                const int *min_nba) {
+  clear_error();
+  RIMP2_REQ(n > 0 && n <= 64 && nvirt_min && min_nocc && min_nba,
+            "rimp2_set_split_kernel_rule: bad table");
+  std::vector<KernelRule> t;
+  for (int k = 0; k < n; ++k) {
+    RIMP2_REQ(min_nocc[k] >= 1 && min_nba[k] >= 1,
+              "rimp2_set_split_kernel_rule: thresholds must be positive");
+    RIMP2_REQ(k == 0 || nvirt_min[k] > nvirt_min[k - 1],
+              "rimp2_set_split_kernel_rule: nvirt_min must increase");
+    t.push_back({nvirt_min[k], min_nocc[k], min_nba[k]});
+  }
+  std::lock_guard<std::mutex> lk(g_bucket_mu);
+  g_krule = t;
+  return RIMP2_OK;
+}
+
+int rimp2_split_kernel_for(int nvirt, int nocc, int NBA) {
+  const int ns = rimp2_split_nslices(nvirt, nocc, NBA);
+  if (ns == 0) return 0;
+  if (ns >= 2) return 1;
+  return rimp2::pair_kernel_for(nocc, nvirt, NBA) ? 2 : 1;
+}
+
 int rimp2_batch_plan_create(void **plan, int nfrag, const int *nocc, const int *nvirt,
                             const int *NBA, const double *const *dCalpha,
                             const double *const *dEVocc, const double *const *dEVvirt,

@@ -172,5 +172,8 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
                long long b_row0, long long b_bstride, int M, int N, int nbatch, double *out,
                long long sOm, long long sOn, long long sOb, cudaStream_t s);
 bool split_supported();
+// Energy kernel of a one-residual-slice fragment: true = paired-CTA kernel
+// (kernel-rule table of capi.cu; RIMP2_PAIR_KERNEL=0/1 overrides it)
+bool pair_kernel_for(int nocc, int nvirt, int NBA);
 
 }  // namespace rimp2

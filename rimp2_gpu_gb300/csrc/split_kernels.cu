@@ -31,7 +31,8 @@
 //   memory.  T1 is read out and released first, so the next item's T1 MMAs
 //   overlap this item's T2 phase; diagonal tile pairs take T2 = T1^T through
 //   shared memory.
-// A one-residual-slice fragment with nocc >= 10 and NBA >= 1024 runs instead
+// A one-residual-slice fragment with enough occupied orbitals and a long
+// enough auxiliary space (the measured kernel table of capi.cu) runs instead
 // on split_pair_kernel: clusters of two CTAs issuing cta_group::2 MMAs over
 // two occupied pairs that share their B operand, with a third slice plane
 // V = fp16(C*s) that folds R1a S0b + R1a R1b into R1a V (three products per
@@ -192,6 +193,12 @@ constexpr uint32_t IDESC = (1u << 4)            // D format F32
 
 // the same with N = 256 (two stacked 128-row B panels)
 constexpr uint32_t IDESC_N256 = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(TILE >> 4) << 24);
+
+// kind::f16, F16 operands, F32 accumulator, K-major, M rows, N columns
+// (M = 128: N a multiple of 16 up to 256)
+__host__ __device__ constexpr uint32_t idesc_mn(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
 
 __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
@@ -2133,21 +2140,6 @@ int launch_pair(const Group &g, PairParams Q, int npair, cudaStream_t s) {
   return RIMP2_OK;
 }
 
-// Kernel choice per one-residual-slice fragment.  The paired-CTA kernel
-// (three products per element pair) runs in 0.87-0.95x the one-CTA kernel's
-// time once NBA >= 1024 (0.87x at nocc=128 nvirt=1024 NBA=4096), but its
-// per-item cost (the exchange-tile transpose, the cross-CTA hand-offs) loses
-// on short auxiliary spaces: 1.14-1.49x at NBA <= 512, even at 1024.  Its
-// dummy CTAs (an odd count of i <= j for some j) add 2 C(nocc) / (nocc
-// (nocc+1)/2) - 1 of work: over 10% below nocc = 10.  RIMP2_PAIR_KERNEL=0 or
-// =1 overrides the choice.
-bool pair_kernel_for(int nocc, int NBA) {
-  const char *e = getenv("RIMP2_PAIR_KERNEL");
-  if (e && e[0] == '0') return false;
-  if (e && e[0] == '1') return true;
-  return nocc >= 10 && NBA >= 1024;
-}
-
 int build_group(Group &g, cudaStream_t s) {
   // heaviest fragments first: their items lead the queue
   std::stable_sort(g.fh.begin(), g.fh.end(),
@@ -2340,7 +2332,15 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
 // transform): D[m][n] = sum_k A[m][k] B[n][k], A and B K-major FP16 slices
 // with per-row power-of-two scales, exact integer L0 + residual L1 in TMEM,
 // FP64 output (L0 and L1 combined in FP64) with arbitrary strides.
-// One output tile (128 x NT, NT <= 128) per CTA.
+// Persistent: each CTA takes output tiles (128 x NT, NT <= 128) blockIdx.x,
+// + gridDim.x, ... (all tiles have the same K), with two TMEM accumulator
+// sets, so that the epilogue of one tile (TMEM -> FP64 stores) runs while
+// the tensor core works on the next and the copy ring never drains between
+// tiles.  Per K16 step one MMA over the stacked B planes [S0b; R1b] (N = 2 NT)
+// gives L0 and S0a R1b, then R1a S0b, R1a R1b (and S0a R2b, R2a S0b with two
+// residual slices) accumulate into L1.
+// Roles: warp 0 TMA producer, warp 1 MMA issuer and TMEM owner, warps 2-5
+// epilogue (one per TMEM lane quadrant).  Every wait is bounded.
 // ==========================================================================
 struct GemmSP {
   int M, N, NT, nks, mtiles, ntiles, nbatch;
@@ -2350,43 +2350,55 @@ struct GemmSP {
   const float *a_inv, *b_inv;      // per-row inverse scales (indexed like the rows)
   double *out;
   long long sOm, sOn, sOb;
-  uint32_t idesc;
+  uint32_t tmem_cols;              // TMEM columns allocated (a power of two >= 4 NT)
   int *err;
 };
+
+constexpr int GEMM_NST = 2;
+constexpr int gemm_stage_bytes(int nsl, int NT) { return nsl * (PANEL_BYTES + NT * 128); }
+constexpr int gemm_smem_bytes(int nsl, int NT) {
+  return GEMM_NST * gemm_stage_bytes(nsl, NT) + 1024 + 256;
+}
 
 template <int NSL>
 __global__ void __launch_bounds__(192, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       GemmSP P) {
-  constexpr int NST = 2;
-  constexpr int SLOT = PANEL_BYTES;                 // 16 KB per panel slot (A or B)
-  constexpr int STAGE_BYTES = NSL * 2 * SLOT;
+  constexpr int NST = GEMM_NST;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t *bars = (uint64_t *)(base + NST * STAGE_BYTES);  // full[2], empty[2], tfull, drain
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NST + 2);
+  const int NT = P.NT;
+  const int BPL = NT * 128;  // bytes of one B plane (NT rows of 64 FP16)
+  const int STAGE = NSL * (PANEL_BYTES + BPL);
+  // bars: full[2], empty[2], tfull[2], tempty[2], drain
+  uint64_t *bars = (uint64_t *)(base + NST * STAGE);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * NST + 5);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[NST]);
-  const uint32_t tfull = smem_u32(&bars[2 * NST]), drain = smem_u32(&bars[2 * NST + 1]);
-  const int item = blockIdx.x;
-  const int b = item / (P.mtiles * P.ntiles);
-  const int rem = item % (P.mtiles * P.ntiles);
-  const int mt = rem / P.ntiles, nt = rem % P.ntiles;
-  const int stage_tx = NSL * (TILE * KSTEP * 2 + P.NT * KSTEP * 2);
+  const uint32_t tfull0 = smem_u32(&bars[2 * NST]), tempty0 = smem_u32(&bars[2 * NST + 2]);
+  const uint32_t drain = smem_u32(&bars[2 * NST + 4]);
+  const long long per_b = (long long)P.mtiles * P.ntiles;
+  const long long nitems = per_b * P.nbatch;
   if (threadIdx.x == 0) {
     for (int st = 0; st < NST; ++st) {
       mbar_init(full0 + 8 * st, 1);
       mbar_init(empty0 + 8 * st, 1);
     }
-    mbar_init(tfull, 1);
+    for (int u = 0; u < 2; ++u) {
+      mbar_init(tfull0 + 8 * u, 1);
+      mbar_init(tempty0 + 8 * u, 4);  // the four epilogue warps
+    }
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-                     smem_u32(tmem_slot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(P.tmem_cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -2394,34 +2406,48 @@ __global__ void __launch_bounds__(192, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const long long arow = P.a_row0 + (long long)b * P.a_bstride + (long long)mt * TILE;
-  const long long brow = P.b_row0 + (long long)b * P.b_bstride + (long long)nt * P.NT;
+  auto tile_rows = [&](long long item, long long &arow, long long &brow, int &b, int &mt, int &nt) {
+    b = (int)(item / per_b);
+    const long long rem = item % per_b;
+    mt = (int)(rem / P.ntiles);
+    nt = (int)(rem % P.ntiles);
+    arow = P.a_row0 + (long long)b * P.a_bstride + (long long)mt * TILE;
+    brow = P.b_row0 + (long long)b * P.b_bstride + (long long)nt * NT;
+  };
   if (warp == 0) {
+    // ------------------------------ TMA producer ------------------------------
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
       int armed[NST] = {-1, -1};
       bool ok = true;
-      for (int kc = 0; kc < P.nks; ++kc) {
-        if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err, 11)) {
-          ok = false;
-          break;
-        }
-        const uint32_t fb = full0 + 8 * stage;
-        mbar_expect_tx(fb, stage_tx);
-        armed[stage] = (int)phase;
-        const uint32_t dst = smem_u32(base + stage * STAGE_BYTES);
+      const uint32_t tx = (uint32_t)STAGE;
+      for (long long item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+        long long arow, brow;
+        int b, mt, nt;
+        tile_rows(item, arow, brow, b, mt, nt);
+        for (int kc = 0; kc < P.nks; ++kc) {
+          if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, P.err, 11)) {
+            ok = false;
+            break;
+          }
+          const uint32_t fb = full0 + 8 * stage;
+          mbar_expect_tx(fb, tx);
+          armed[stage] = (int)phase;
+          const uint32_t dst = smem_u32(base + stage * STAGE);
 #pragma unroll
-        for (int sl = 0; sl < NSL; ++sl) {
-          tma_load_3d(dst + (2 * sl) * SLOT, &tmA, fb, 0, (int)(kc * P.a_ncol + arow), sl);
-          tma_load_3d(dst + (2 * sl + 1) * SLOT, &tmB, fb, 0, (int)(kc * P.b_ncol + brow), sl);
-        }
-        if (++stage == NST) {
-          stage = 0;
-          phase ^= 1;
+          for (int sl = 0; sl < NSL; ++sl) {  // A planes, then the B planes back to back
+            tma_load_3d(dst + sl * PANEL_BYTES, &tmA, fb, 0, (int)(kc * P.a_ncol + arow), sl);
+            tma_load_3d(dst + NSL * PANEL_BYTES + sl * BPL, &tmB, fb, 0,
+                        (int)(kc * P.b_ncol + brow), sl);
+          }
+          if (++stage == NST) {
+            stage = 0;
+            phase ^= 1;
+          }
         }
       }
-      if (!ok) {
+      if (!ok || *abort_flag) {  // copies in flight land before the CTA can exit
         for (int st = 0; st < NST; ++st) {
           if (armed[st] < 0) continue;
           const long long t0 = clock64();
@@ -2431,78 +2457,106 @@ __global__ void __launch_bounds__(192, 1)
       }
     }
   } else if (warp == 1) {
+    // ------------------------------ MMA issuer --------------------------------
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
-      const uint32_t dL0 = tmem, dL1 = tmem + TILE;
-      for (int kc = 0; kc < P.nks; ++kc) {
-        if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err, 12)) {
+      const uint32_t id2 = idesc_mn(TILE, 2 * NT), id1 = idesc_mn(TILE, NT);
+      long long t = 0;  // tiles of this CTA so far
+      for (long long item = blockIdx.x; item < nitems && ok; item += gridDim.x, ++t) {
+        const int u = (int)(t & 1);
+        // the epilogue has read this accumulator set's previous tile
+        if (t >= 2 &&
+            !mbar_wait(tempty0 + 8 * u, (uint32_t)(((t >> 1) - 1) & 1), abort_flag, P.err, 14)) {
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t sb = smem_u32(base + stage * STAGE_BYTES);
+        const uint32_t dL0 = tmem + (uint32_t)(u * 2 * NT), dL1 = dL0 + (uint32_t)NT;
+        for (int kc = 0; kc < P.nks; ++kc) {
+          if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, P.err, 12)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = smem_u32(base + stage * STAGE);
+          const uint32_t sb = sa + NSL * PANEL_BYTES;
 #pragma unroll
-        for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
-          const uint32_t koff = k16 * 32;
-          const uint64_t a0 = smem_desc(sb + 0 * SLOT + koff), b0 = smem_desc(sb + 1 * SLOT + koff);
-          const uint64_t a1 = smem_desc(sb + 2 * SLOT + koff), b1 = smem_desc(sb + 3 * SLOT + koff);
-          const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
-          mma_f16_id(dL0, a0, b0, P.idesc, acc);
-          mma_f16_id(dL1, a0, b1, P.idesc, acc);
-          mma_f16_id(dL1, a1, b0, P.idesc, 1u);
-          mma_f16_id(dL1, a1, b1, P.idesc, 1u);
-          if (NSL > 2) {
-            const uint64_t a2 = smem_desc(sb + 4 * SLOT + koff), b2 = smem_desc(sb + 5 * SLOT + koff);
-            mma_f16_id(dL1, a0, b2, P.idesc, 1u);
-            mma_f16_id(dL1, a2, b0, P.idesc, 1u);
+          for (int k16 = 0; k16 < KSTEP / 16; ++k16) {
+            const uint32_t koff = k16 * 32;
+            const uint64_t a0 = smem_desc(sa + koff), a1 = smem_desc(sa + PANEL_BYTES + koff);
+            const uint64_t b0 = smem_desc(sb + koff), b1 = smem_desc(sb + BPL + koff);
+            const uint32_t acc = (kc > 0 || k16 > 0) ? 1u : 0u;
+            mma_f16_id(dL0, a0, b0, id2, acc);  // [L0 | L1] = S0a [S0b; R1b]
+            mma_f16_id(dL1, a1, b0, id1, 1u);   // R1a S0b
+            mma_f16_id(dL1, a1, b1, id1, 1u);   // R1a R1b
+            if (NSL > 2) {
+              const uint64_t a2 = smem_desc(sa + 2 * PANEL_BYTES + koff);
+              const uint64_t b2 = smem_desc(sb + 2 * BPL + koff);
+              mma_f16_id(dL1, a0, b2, id1, 1u);  // S0a R2b
+              mma_f16_id(dL1, a2, b0, id1, 1u);  // R2a S0b
+            }
+          }
+          mma_commit(empty0 + 8 * stage);
+          if (++stage == NST) {
+            stage = 0;
+            phase ^= 1;
           }
         }
-        mma_commit(empty0 + 8 * stage);
-        if (++stage == NST) {
-          stage = 0;
-          phase ^= 1;
-        }
+        if (!ok) break;
+        mma_commit(tfull0 + 8 * u);
       }
-      if (ok) mma_commit(tfull);
       mma_commit(drain);
       const long long t0 = clock64();
       while (!mbar_test(drain, 0) && clock64() - t0 < WAIT_BUDGET) {
       }
     }
   } else {
+    // ------------------------------ epilogue ----------------------------------
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
-    const long long m = (long long)mt * TILE + row;
-    if (mbar_wait(tfull, 0, abort_flag, P.err, 13)) {
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    long long t = 0;
+    for (long long item = blockIdx.x; item < nitems; item += gridDim.x, ++t) {
+      const int u = (int)(t & 1);
+      if (!mbar_wait(tfull0 + 8 * u, (uint32_t)((t >> 1) & 1), abort_flag, P.err, 13)) break;
       tc_fence_after();
+      long long arow, brow;
+      int b, mt, nt;
+      tile_rows(item, arow, brow, b, mt, nt);
+      const long long m = (long long)mt * TILE + row;
       const double sa = (double)P.a_inv[arow + row];
-      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16);
+      const uint32_t taddr = tmem + lane_off + (uint32_t)(u * 2 * NT);
       double *orow = P.out + (long long)b * P.sOb + m * P.sOm;
-      for (int c0 = 0; c0 < P.NT; c0 += 16) {
+      for (int c0 = 0; c0 < NT; c0 += 16) {
         float l0[16], l1[16];
         tmem_ld16(taddr + c0, l0);
-        tmem_ld16(taddr + TILE + c0, l1);
+        tmem_ld16(taddr + NT + c0, l1);
         tmem_wait_ld();
         if (m < P.M) {
 #pragma unroll
           for (int k = 0; k < 16; ++k) {
-            const int n = nt * P.NT + c0 + k;
-            if (c0 + k < P.NT && n < P.N) {
+            const int n = nt * NT + c0 + k;
+            if (n < P.N) {
               const double sb = (double)P.b_inv[brow + c0 + k];
               orow[(long long)n * P.sOn] = ((double)l0[k] + (double)l1[k]) * (sa * sb);
             }
           }
         }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty0 + 8 * u);
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(P.tmem_cols)
+                 : "memory");
   }
 }
 
@@ -2642,6 +2696,21 @@ __device__ __forceinline__ bool conv_any(bool p) {
       "selp.u32 %0, 1, 0, o;\n\t}"
       : "=r"(r)
       : "r"((uint32_t)p), "r"(32 * AH_CONV)
+      : "memory");
+  return r != 0;
+}
+
+// Bounded vote over the 128 converter threads of row group g (the four warps
+// that hold the same tile rows; named barrier 3 + g).
+__device__ __forceinline__ bool group_any(bool p, int g) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, o;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred o, %2, 128, q;\n\t"
+      "selp.u32 %0, 1, 0, o;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(3 + g)
       : "memory");
   return r != 0;
 }
@@ -2814,7 +2883,10 @@ __global__ void __maxnreg__(96)
       smx[(b * 4 + kq) * 128 + r] = key;
       bool ok = true;
       if (c >= 2) ok = mbar_wait(sempty0 + 8 * b, (uint32_t)(((c - 2) >> 1) & 1), abort_flag, P.err, 21);
-      if (conv_any(!ok)) {  // also the barrier of the max exchange
+      // the four warps of a row group exchange their K quarters' maxima; the
+      // groups do not wait for one another, so their latency-bound phases
+      // (loads, slicing, TMEM round trips) interleave
+      if (group_any(!ok, warp & 3)) {
         ok_all = false;
         break;
       }
@@ -2862,16 +2934,16 @@ __global__ void __maxnreg__(96)
       // the next iteration's start (the L2 prefetch keeps their latency short)
       if (c + 1 < nks) issue_chunk(c + 1);
       // the previous chunk's epilogue runs while this chunk's MMAs do
-      if (c >= 1 && conv_any(!epilogue(c - 1))) {
+      if (c >= 1 && group_any(!epilogue(c - 1), warp & 3)) {
         ok_all = false;
         break;
       }
     }
     // copies still in flight land before the CTA may exit
     asm volatile("cp.async.wait_all;" ::: "memory");
-    if (ok_all && conv_any(!epilogue(nks - 1))) ok_all = false;
+    const bool last_ok = ok_all && epilogue(nks - 1);
+    ok_all = !conv_any(!last_ok);  // every converter thread reaches this vote
     if (ok_all) {
-      asm volatile("bar.sync 2, %0;" ::"r"(32 * AH_CONV) : "memory");
       const double *stg = reinterpret_cast<const double *>(stages);
       for (int idx = threadIdx.x; idx < P.nocc * AH_TA * AH_TM; idx += 32 * AH_CONV) {
         const int ml = idx & 7, al = (idx >> 3) & 15, n = idx >> 7;
@@ -3200,7 +3272,7 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
     F.Epair = Epair[f];
     F.Etot = Etot[f];
     const int ns = nslices ? nslices[f] : 1;
-    P->g[ns >= 2 ? 1 : (pair_kernel_for(F.nocc, F.NBA) ? 2 : 0)].fh.push_back(F);
+    P->g[ns >= 2 ? 1 : (pair_kernel_for(F.nocc, F.nvirt, F.NBA) ? 2 : 0)].fh.push_back(F);
   }
   for (auto &g : P->g) {
     if (g.fh.empty()) continue;
@@ -3560,7 +3632,9 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
   P.sOm = sOm;
   P.sOn = sOn;
   P.sOb = sOb;
-  P.idesc = (1u << 4) | ((uint32_t)(P.NT >> 3) << 17) | ((uint32_t)(TILE >> 4) << 24);
+  uint32_t cols = 32;
+  while (cols < (uint32_t)(4 * P.NT)) cols <<= 1;
+  P.tmem_cols = cols;
   P.err = device_error_word();
   const long long nitems = (long long)nbatch * P.mtiles * P.ntiles;
   if (nitems > 2147483647LL) {
@@ -3570,16 +3644,17 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
   CUtensorMap tA, tB;
   RIMP2_TRY(encode_op(tA, A, TILE));
   RIMP2_TRY(encode_op(tB, B, P.NT));
-  const int smem = 2 * A.nsl * 2 * PANEL_BYTES + 1024 + 256;
-  if (A.nsl == 3) {
-    RIMP2_CK(cudaFuncSetAttribute(split_gemm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  smem));
-    split_gemm_kernel<3><<<(unsigned)nitems, 192, smem, s>>>(tA, tB, P);
-  } else {
-    RIMP2_CK(cudaFuncSetAttribute(split_gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  smem));
-    split_gemm_kernel<2><<<(unsigned)nitems, 192, smem, s>>>(tA, tB, P);
-  }
+  const int smem = gemm_smem_bytes(A.nsl, P.NT);
+  auto kern = A.nsl == 3 ? split_gemm_kernel<3> : split_gemm_kernel<2>;
+  RIMP2_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int dev = 0, nsm = 0, resident = 0;
+  RIMP2_CK(cudaGetDevice(&dev));
+  RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 192, smem));
+  // persistent CTAs whose TMEM allocations fit an SM together
+  resident = std::max(1, std::min(resident, (int)(512 / cols)));
+  const long long grid = std::min<long long>(nitems, (long long)nsm * resident);
+  kern<<<(unsigned)grid, 192, smem, s>>>(tA, tB, P);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;
@@ -3594,6 +3669,8 @@ int ao_half_fused(const double *ao, int NBA, int nbas, const double *Cmo, int no
   *handled = false;
   const int NT = (nocc + 15) / 16 * 16;
   if (NT > AH_NT_MAX || nocc <= 0) return RIMP2_OK;
+  const char *env = getenv("RIMP2_AO_FUSED");  // =0: the sliced first half (for comparisons)
+  if (env && env[0] == '0') return RIMP2_OK;
   auto encode = get_encode();
   if (!encode) {
     set_error("cuTensorMapEncodeTiled entry point unavailable");

@@ -94,11 +94,21 @@ def test_bucket_table_roundtrip():
 
 def test_batch_plan_all_four_groups():
     """One plan with a fragment in each launch group: paired-CTA kernel
-    (one residual slice, nocc >= 10, NBA >= 1024), one-CTA kernel with one
-    and with two residual slices, and plain FP64 -- one persistent launch
-    sequence per group, every fragment against the oracle."""
+    (one residual slice; the kernel table set to nocc >= 10, NBA >= 1024
+    here), one-CTA kernel with one and with two residual slices, and plain
+    FP64 -- one persistent launch sequence per group, every fragment against
+    the oracle."""
+    import os
     import torch
-    from rimp2_gpu_gb300 import api
+    from rimp2_gpu_gb300 import api, autotune
+    api.set_split_kernel_rule([0], [10], [1024])
+    try:
+        _all_four_groups(api, torch)
+    finally:
+        autotune.load(os.path.join(os.path.dirname(api.__file__), "tuning", "split_buckets.json"))
+
+
+def _all_four_groups(api, torch):
     shapes = [(12, 256, 1024, 1), (11, 200, 300, 1), (5, 130, 777, 2), (8, 64, 256, 0)]
     dev, ref = [], []
     for k, (nocc, nvirt, NBA, _) in enumerate(shapes):

@@ -222,3 +222,77 @@ def test_fortran_module_matches_header():
         nargs = 0 if not args.strip() else args.count(",") + 1
         assert nargs == protos[cname], f"{cname}: {nargs} Fortran arguments, {protos[cname]} in C"
         assert hasattr(lib, cname), f"{cname} is not exported"
+
+
+def test_kernel_rule_table(monkeypatch):
+    """The energy-kernel table of the one-residual-slice split form is a
+    host-side lookup: per virtual bucket, the paired-CTA kernel where nocc
+    and NBA reach the bucket's thresholds; two-slice shapes run the one-CTA
+    kernel, tiny ones the FP64 tier; the environment overrides the table."""
+    from rimp2_gpu_gb300 import api, _lib
+    monkeypatch.delenv("RIMP2_PAIR_KERNEL", raising=False)
+    api.set_split_buckets([0, 16, 128, 192], [0, 2, 2, 1])
+    try:
+        api.set_split_kernel_rule([0, 256], [10, 4], [1024, 512])
+        assert api.split_kernel_for(200, 12, 1024) == 2
+        assert api.split_kernel_for(200, 8, 2048) == 1   # nocc below the first bucket's 10
+        assert api.split_kernel_for(200, 12, 512) == 1   # NBA below 1024
+        assert api.split_kernel_for(300, 4, 512) == 2    # second bucket
+        assert api.split_kernel_for(300, 3, 4096) == 1
+        assert api.split_kernel_for(100, 40, 4096) == 1  # two residual slices: one-CTA only
+        assert api.split_kernel_for(8, 4, 4096) == 0     # FP64 tier
+        monkeypatch.setenv("RIMP2_PAIR_KERNEL", "1")
+        assert api.split_kernel_for(300, 3, 64) == 2
+        monkeypatch.setenv("RIMP2_PAIR_KERNEL", "0")
+        assert api.split_kernel_for(200, 12, 1024) == 1
+        monkeypatch.delenv("RIMP2_PAIR_KERNEL")
+        for bad in (([0, 0], [10, 4], [1024, 512]), ([0], [0], [1024]), ([0], [10], [0])):
+            with pytest.raises(_lib.Rimp2Error):
+                api.set_split_kernel_rule(*bad)
+    finally:
+        from rimp2_gpu_gb300 import autotune
+        autotune.load(os.path.join(ROOT, "rimp2_gpu_gb300", "tuning", "split_buckets.json"))
+
+
+def test_kernel_rule_fit():
+    """The autotuner keeps the thresholds that minimise the summed time of
+    its grid, and 'never' when the paired kernel wins nowhere."""
+    from rimp2_gpu_gb300 import autotune as A
+    grid = [{"nocc": o, "NBA": b, "one_ms": 1.0,
+             "pair_ms": 0.8 if (o >= 12 and b >= 2048) else 1.3}
+            for o in A.KGRID_NOCC for b in A.KGRID_NBA]
+    t, mo, mb = A._fit_rule(grid)
+    assert (mo, mb) == (12, 2048)
+    assert abs(t - (len(grid) - 0.2 * 3 * 2)) < 1e-9
+    for g in grid:
+        g["pair_ms"] = 2.0
+    _, mo, mb = A._fit_rule(grid)
+    assert mo == A.NEVER or mb == A.NEVER
+
+
+def test_tuned_tables_match_library_defaults():
+    """The library's built-in tables are the committed autotuner output."""
+    import json
+    import subprocess
+    import sys
+    t = json.load(open(os.path.join(ROOT, "rimp2_gpu_gb300", "tuning", "split_buckets.json")))
+    code = ("from rimp2_gpu_gb300 import api\n"
+            "import json, sys\n"
+            "t = json.loads(sys.argv[1])\n"
+            "for b in t['buckets']:\n"
+            "    assert api.split_nslices(max(b['nvirt_min'], 64), 4, 64) == b['nslices'] or "
+            "b['nvirt_min'] < 16, b\n"
+            "for r in t.get('kernel_rule', []):\n"
+            "    if r['nvirt_min'] == 0: continue\n"
+            "    nv = r['nvirt_min']\n"
+            "    if api.split_nslices(nv, 64, 4096) != 1: continue\n"
+            "    mo, mb = r['min_nocc'], r['min_nba']\n"
+            "    if mo < 65536 and mb < 65536:\n"
+            "        assert api.split_kernel_for(nv, mo, mb) == 2, r\n"
+            "    if mo > 1 and mo < 65536:\n"
+            "        assert api.split_kernel_for(nv, mo - 1, max(mb, 1) if mb < 65536 else 64) == 1, r\n"
+            "    if mb > 1 and mb < 65536:\n"
+            "        assert api.split_kernel_for(nv, max(mo, 64) if mo < 65536 else 64, mb - 1) == 1, r\n")
+    out = subprocess.run([sys.executable, "-c", code, json.dumps(t)], cwd=ROOT,
+                         capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr

@@ -168,6 +168,37 @@ def test_pair_kernel_within_1e7(api, kernel_choice, nocc, nvirt, NBA):
     assert (np.abs(Ep - Ep1) / np.abs(Ep1)).max() <= 1e-7
 
 
+# valid counts of the last 128-wide virtual block (zero-padded columns in
+# its tiles): one, around the 16-column steps, half, and one short of full
+SHORT_BLOCK = [1, 15, 16, 17, 40, 64, 65, 100, 112, 113, 127]
+
+
+@pytest.mark.parametrize("rem", SHORT_BLOCK)
+def test_short_last_block_both_kernels(api, kernel_choice, rem):
+    """Fragments whose last 128-wide virtual block holds `rem` valid columns,
+    against the CPU oracle: with one residual slice (nvirt = 256 + rem, in
+    the one-slice bucket) on the paired kernel and on the one-CTA kernel --
+    off-diagonal tile pairs with one short block and the short diagonal
+    pair -- and with two residual slices on the one-CTA kernel beside one
+    full block (128 + rem) and alone (rem >= 16)."""
+    nocc, NBA = 7, 200
+    runs = [(256 + rem, "1", 1), (256 + rem, "0", 1), (128 + rem, "0", 2)]
+    if rem >= 16:
+        runs.append((rem, "0", 2))
+    ref = {}
+    for nvirt, kern, ns in runs:
+        if nvirt not in ref:
+            Ca, eo, ev = O.gen_fragment(1100 + nvirt, nocc, nvirt, NBA)
+            ref[nvirt] = (Ca, eo, ev) + O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+        Ca, eo, ev, Epr, Er = ref[nvirt]
+        kernel_choice(kern)
+        Ep, E = dev_energy(api, Ca, eo, ev, ns)
+        assert api.last_split_kernel() == (2 if kern == "1" else 1)
+        rel = np.abs(Ep - Epr) / np.abs(Epr)
+        assert rel.max() <= 1e-7, (nvirt, kern, ns, rel.max())
+        assert abs(E - Er) <= 1e-7 * abs(Er)
+
+
 def test_pair_kernel_batched(api, kernel_choice):
     """Uneven fragments through one paired-CTA launch (graph-captured plan)."""
     import torch
@@ -193,9 +224,20 @@ def test_pair_kernel_batched(api, kernel_choice):
 
 
 def test_kernel_choice_is_reported(api, kernel_choice):
-    """One-residual-slice fragments with nocc >= 10 and NBA >= 1024 run the
-    paired kernel, the rest the one-CTA kernel; the environment overrides the
-    choice and the library says which kernel ran."""
+    """One-residual-slice fragments run the kernel the table picks (set here
+    to the paired kernel for nocc >= 10 and NBA >= 1024), the rest the
+    one-CTA kernel; the environment overrides the choice and the library
+    says which kernel ran."""
+    import os
+    from rimp2_gpu_gb300 import autotune
+    api.set_split_kernel_rule([0], [10], [1024])
+    try:
+        _kernel_choice_checks(api, kernel_choice)
+    finally:
+        autotune.load(os.path.join(os.path.dirname(api.__file__), "tuning", "split_buckets.json"))
+
+
+def _kernel_choice_checks(api, kernel_choice):
     small = O.gen_fragment(31, 6, 200, 256)
     big = O.gen_fragment(32, 32, 130, 1024)
     kernel_choice("")
