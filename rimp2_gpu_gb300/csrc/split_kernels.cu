@@ -2649,24 +2649,33 @@ __device__ __forceinline__ void tmem_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-// split_int with the integer part formed without an int->float conversion
-// (those run at a fraction of the FP32 rate): for 0 <= qi < 2^23 the float
-// with bits 0x4B000000 | qi is 2^23 + qi exactly, so subtracting 2^23 gives
-// qi.  Same results as split_int.
-__device__ __forceinline__ void split_int_fast(unsigned long long b, int e, float &q, float &r) {
-  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
-  const int ed = (int)(mag >> 52);
-  const int sh = 1075 - 32 - ed - e;
-  unsigned long long A = 0;
-  if (ed != 0 && sh < 64) {
-    const unsigned long long M = (mag & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-    A = sh >= 0 ? (M >> sh) : (M << (-sh));
-  }
-  const unsigned long long qi = (A + 0x7FFFFFFFull + ((A >> 32) & 1ull)) >> 32;
-  const long long fr = (long long)A - (long long)(qi << 32);
-  const uint32_t sgn = (uint32_t)(b >> 63) << 31;
-  q = __uint_as_float(__float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)qi) - 8388608.0f) | sgn);
-  r = __uint_as_float(__float_as_uint((float)(int)(fr >> 1) * 4.656612873077393e-10f) ^ sgn);
+// Split of a double x with |x 2^e| <= 511.5 into q (an integer, |q| <= 512,
+// rounded half to even) and r ~ x 2^e - q in FP32 arithmetic only (GB300's
+// FP64 pipe is a small fraction of the FP32 one): v = |x| 2^e is the float
+// f_hi holding the top 24 significant bits of x (exponent and fraction bits
+// moved into place, no rounding) plus f_lo holding the next 23 bits (a 23-bit
+// integer formed with the 2^23 magic constant, times a power of two);
+// q = round(f_hi) with the 1.5 * 2^23 constant, r = (f_hi - q) + f_lo, where
+// f_hi - q is exact and the sum rounds once (2^-25 of |r|).  Values below
+// 2^-40 of the scaled unit, zeros and subnormals give q = r = 0.  The sign
+// of x goes onto both.  Equal to split_int's results to within its rounding
+// of r (checked by emulation of these float operations against exact
+// rational arithmetic).
+__device__ __forceinline__ void split_f32(double x, int e, float &q, float &r) {
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const uint32_t sgn = hi & 0x80000000u;
+  const int ed = (int)((hi >> 20) & 0x7FFu);
+  const int E = ed - 1023 + e;  // |x| 2^e = 1.f 2^E
+  const bool live = ed != 0 && E >= -40;
+  const int Ec = live ? E : 0;
+  const uint32_t frac23 = (__funnelshift_l(lo, hi, 3)) & 0x7FFFFFu;
+  const float fhi = __uint_as_float(((uint32_t)(Ec + 127) << 23) | frac23);
+  const float lo23 = __uint_as_float(0x4B000000u | ((lo >> 6) & 0x7FFFFFu)) - 8388608.0f;
+  const float flo = lo23 * __uint_as_float((uint32_t)(Ec - 46 + 127) << 23);
+  const float qm = (fhi + 12582912.0f) - 12582912.0f;
+  const float rm = (fhi - qm) + flo;
+  q = live ? __uint_as_float(__float_as_uint(qm) | sgn) : 0.0f;
+  r = live ? __uint_as_float(__float_as_uint(rm) ^ sgn) : 0.0f;
 }
 
 // Exponent e with |x| 2^e <= 511.5 (to within 2^-11) for the largest
@@ -2824,6 +2833,10 @@ __global__ void __maxnreg__(96)
       double *stg = reinterpret_cast<double *>(stages);
       for (int col = col0; col < col0 + ncol; col += 4) {
         float l0[4], l1[4], hi[4], lo[4];
+        // the four column scales of the chunk in one 16-byte load (NT and
+        // col are multiples of 4)
+        const float4 sb4 = *reinterpret_cast<const float4 *>(sbc + col);
+        const float sbk[4] = {sb4.x, sb4.y, sb4.z, sb4.w};
         tmem_ld4(tL0 + col, l0);
         tmem_ld4(tL0 + NT + col, l1);
         if (ce > 0) {
@@ -2833,7 +2846,7 @@ __global__ void __maxnreg__(96)
         tmem_wait_ld();
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const float sc = sa * sbc[col + k];  // power of two: the products below are exact
+          const float sc = sa * sbk[k];  // power of two: the products below are exact
           const float xh = l0[k] * sc, xl = l1[k] * sc;
           if (ce == 0) {
             hi[k] = xh;
@@ -2904,8 +2917,8 @@ __global__ void __maxnreg__(96)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {  // two values at a time, packed conversions
           float qa, ra, qb, rb;
-          split_int_fast((unsigned long long)__double_as_longlong(v[8 * g + 2 * q]), e, qa, ra);
-          split_int_fast((unsigned long long)__double_as_longlong(v[8 * g + 2 * q + 1]), e, qb, rb);
+          split_f32(v[8 * g + 2 * q], e, qa, ra);
+          split_f32(v[8 * g + 2 * q + 1], e, qb, rb);
           h0[q] = __floats2half2_rn(qa, qb);  // |q| <= 512: exact in FP16
           h1[q] = __floats2half2_rn(ra, rb);
           const float2 f1 = __half22float2(h1[q]);

@@ -268,15 +268,16 @@ def test_pair_kernel_host_streamed(api, kernel_choice, nocc, nvirt, NBA):
     assert abs(E - Er) <= 1e-7 * abs(Er)
 
 
-def test_pair_kernel_long_K_against_oracle(api):
-    """A long auxiliary space on the library's default kernel choice: nocc=12,
-    nvirt=512, NBA=4096 runs the paired-CTA kernel (one residual slice) with
-    64 K chunks per product chain, the regime of the large single fragment.
-    Every pair energy against the CPU oracle (the alpha loop of RIMP2.F90:
-    395-405 restated, with the MP2 energy), split at 1e-7 and the plain FP64
-    kernel at 1e-11, in the manner of the reference's own Debug self-check
-    (RIMP2.F90:253-367)."""
+def test_pair_kernel_long_K_against_oracle(api, kernel_choice):
+    """A long auxiliary space on the paired-CTA kernel (one residual slice,
+    forced: the kernel table starts it at nocc >= 16 for this bucket):
+    nocc=12, nvirt=512, NBA=4096, 64 K chunks per product chain, the regime
+    of the large single fragment.  Every pair energy against the CPU oracle
+    (the alpha loop of RIMP2.F90:395-405 restated, with the MP2 energy),
+    split at 1e-7 and the plain FP64 kernel at 1e-11, in the manner of the
+    reference's own Debug self-check (RIMP2.F90:253-367)."""
     nocc, nvirt, NBA = 12, 512, 4096
+    kernel_choice("1")
     Ca, eo, ev = O.gen_fragment(61, nocc, nvirt, NBA)
     Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
     Ep, E = api.energy(nvirt, nocc, NBA, Ca, eo, ev, precision=api.PREC_SPLIT)
