@@ -2339,8 +2339,11 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
 // tiles.  Per K16 step one MMA over the stacked B planes [S0b; R1b] (N = 2 NT)
 // gives L0 and S0a R1b, then R1a S0b, R1a R1b (and S0a R2b, R2a S0b with two
 // residual slices) accumulate into L1.
-// Roles: warp 0 TMA producer, warp 1 MMA issuer and TMEM owner, warps 2-5
-// epilogue (one per TMEM lane quadrant).  Every wait is bounded.
+// Roles: warp 0 TMA producer, warp 1 MMA issuer and TMEM owner, warps 2-9
+// epilogue (two per TMEM lane quadrant, alternate 16-column chunks).  The
+// epilogue scales L0 and L1 by the row and column powers of two in FP32
+// (exact) and adds them once in FP64: GB300's FP64 pipe is slow, and it
+// bounds this kernel's epilogue.  Every wait is bounded.
 // ==========================================================================
 struct GemmSP {
   int M, N, NT, nks, mtiles, ntiles, nbatch;
@@ -2360,8 +2363,10 @@ constexpr int gemm_smem_bytes(int nsl, int NT) {
   return GEMM_NST * gemm_stage_bytes(nsl, NT) + 1024 + 256;
 }
 
+constexpr int GEMM_THREADS = 64 + 32 * 8;
+
 template <int NSL>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       GemmSP P) {
   constexpr int NST = GEMM_NST;
@@ -2387,7 +2392,7 @@ __global__ void __launch_bounds__(192, 1)
     }
     for (int u = 0; u < 2; ++u) {
       mbar_init(tfull0 + 8 * u, 1);
-      mbar_init(tempty0 + 8 * u, 4);  // the four epilogue warps
+      mbar_init(tempty0 + 8 * u, 8);  // the eight epilogue warps
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -2515,6 +2520,7 @@ __global__ void __launch_bounds__(192, 1)
   } else {
     // ------------------------------ epilogue ----------------------------------
     const int quad = warp & 3;
+    const int half = (warp - 2) >> 2;  // 16-column chunks half, half + 2, ...
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     long long t = 0;
@@ -2526,10 +2532,10 @@ __global__ void __launch_bounds__(192, 1)
       int b, mt, nt;
       tile_rows(item, arow, brow, b, mt, nt);
       const long long m = (long long)mt * TILE + row;
-      const double sa = (double)P.a_inv[arow + row];
+      const float sa = P.a_inv[arow + row];
       const uint32_t taddr = tmem + lane_off + (uint32_t)(u * 2 * NT);
       double *orow = P.out + (long long)b * P.sOb + m * P.sOm;
-      for (int c0 = 0; c0 < NT; c0 += 16) {
+      for (int c0 = 16 * half; c0 < NT; c0 += 32) {
         float l0[16], l1[16];
         tmem_ld16(taddr + c0, l0);
         tmem_ld16(taddr + NT + c0, l1);
@@ -2539,8 +2545,17 @@ __global__ void __launch_bounds__(192, 1)
           for (int k = 0; k < 16; ++k) {
             const int n = nt * NT + c0 + k;
             if (n < P.N) {
-              const double sb = (double)P.b_inv[brow + c0 + k];
-              orow[(long long)n * P.sOn] = ((double)l0[k] + (double)l1[k]) * (sa * sb);
+              const float sb = P.b_inv[brow + c0 + k];
+              const float sc = sa * sb;  // a power of two
+              double v;
+              if (sc >= 0x1p-100f) {
+                // l0 (an integer below 2^24) and l1 times sc are exact
+                // floats; one FP64 addition, rounded as (l0 + l1) sc
+                v = (double)(l0[k] * sc) + (double)(l1[k] * sc);
+              } else {  // scales too small for FP32: the same sum in FP64
+                v = ((double)l0[k] + (double)l1[k]) * ((double)sa * (double)sb);
+              }
+              orow[(long long)n * P.sOn] = v;
             }
           }
         }
@@ -2724,8 +2739,10 @@ __device__ __forceinline__ bool group_any(bool p, int g) {
   return r != 0;
 }
 
+template <bool AO_TMA>
 __global__ void __maxnreg__(96)
-    ao_half_kernel(const __grid_constant__ CUtensorMap tmB, AoHalfParams P) {
+    ao_half_kernel(const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmAO,
+                   AoHalfParams P) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int NT = P.NT;
@@ -2736,12 +2753,14 @@ __global__ void __maxnreg__(96)
   uint32_t *smx = (uint32_t *)(base + 2 * STAGE + AH_SLOT_BYTES);  // [2 parity][4 quarter][128]
   float *sscale = (float *)(smx + 2 * 4 * 128);                    // [2][128]
   uint64_t *bars = (uint64_t *)(sscale + 2 * 128);
-  // bars: stage_full[2], stage_empty[2], acc_full[2], acc_empty[2], drain
-  uint32_t *tmem_slot = (uint32_t *)(bars + 9);
+  // bars: stage_full[2], stage_empty[2], acc_full[2], acc_empty[2], drain,
+  //       ao_full[4] (the AO chunk of each row group, TMA form)
+  uint32_t *tmem_slot = (uint32_t *)(bars + 13);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
   const uint32_t sfull0 = smem_u32(&bars[0]), sempty0 = smem_u32(&bars[2]);
   const uint32_t afull0 = smem_u32(&bars[4]), aempty0 = smem_u32(&bars[6]);
   const uint32_t drain = smem_u32(&bars[8]);
+  const uint32_t aofull0 = smem_u32(&bars[9]);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ta = blockIdx.x % P.ta_tiles, tm = blockIdx.x / P.ta_tiles;
   const int alpha0 = ta * AH_TA, mu0 = tm * AH_TM;
@@ -2755,9 +2774,11 @@ __global__ void __maxnreg__(96)
       mbar_init(aempty0 + 8 * b, AH_CONV);      // converter warps, after reading the chunk
     }
     mbar_init(drain, 1);
+    for (int g = 0; g < 4; ++g) mbar_init(aofull0 + 8 * g, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+    if (AO_TMA) asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmAO) : "memory");
   }
   if (warp == AH_CONV) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
@@ -2785,9 +2806,28 @@ __global__ void __maxnreg__(96)
     const int within = r & 7;
     int armed = -1;  // thread 0: parity of the last stage it armed for the B copy
     int armed_b = 0;
-    // this thread's 16 values of a chunk in the FP64 slot: k = 16 kq + j
-    double *myslot = slot + (16 * kq) * 128 + r;
+    // this thread's 16 values of a chunk in the FP64 slot: k = 16 kq + j.
+    // cp.async form: [k][row]; TMA form: one 16 KB box per row group g
+    // (16 alpha x 64 k x 2 mu, alpha fastest), value (a_l, k, m_l) at
+    // g * 2048 + ((m_l & 1) * 64 + k) * 16 + a_l
+    const int rg = warp & 3;
+    double *myslot = AO_TMA ? slot + rg * 2048 + ((m_l & 1) * 64 + 16 * kq) * 16 + a_l
+                            : slot + (16 * kq) * 128 + r;
+    const int jstride = AO_TMA ? 16 : 128;
     const uint32_t myslot_s = smem_u32(myslot);
+    const uint32_t aofull = aofull0 + 8 * rg;
+    // TMA form: lane 0 of the group's K-quarter-0 warp issues the group's box
+    const bool ao_issuer = AO_TMA && kq == 0 && lane == 0;
+    int ao_pending = -1;  // parity of a box in flight (issuer)
+    auto issue_box = [&](int c) {
+      mbar_expect_tx(aofull, AH_TA * KSTEP * 2 * 8);
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+          " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(slot + rg * 2048)),
+          "l"((uint64_t)&tmAO), "r"(aofull), "r"(alpha0), "r"(c * KSTEP), "r"(mu0 + 2 * rg)
+          : "memory");
+      ao_pending = c & 1;
+    };
     // L2 prefetch of a later chunk: thread t covers the 16-alpha run (128
     // bytes, at most two lines) of k = t / 8 and mu = mu0 + t % 8, so that
     // the chunk's cp.async copies find their data in L2; with one chunk in
@@ -2876,16 +2916,26 @@ __global__ void __maxnreg__(96)
       return true;
     };
     bool ok_all = true;
-    if (nks > 1) prefetch_chunk(1);
-    issue_chunk(0);
+    if (AO_TMA) {
+      if (ao_issuer) issue_box(0);
+    } else {
+      if (nks > 1) prefetch_chunk(1);
+      issue_chunk(0);
+    }
     for (int c = 0; c < nks; ++c) {
-      if (c + 2 < nks) prefetch_chunk(c + 2);
       const int b = c & 1;
-      // chunk c has landed (each thread reads only the values it copied)
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      bool landed = true;
+      if (AO_TMA) {
+        landed = mbar_wait(aofull, (uint32_t)(c & 1), abort_flag, P.err, 26);
+        if (ao_issuer && landed) ao_pending = -1;
+      } else {
+        if (c + 2 < nks) prefetch_chunk(c + 2);
+        // chunk c has landed (each thread reads only the values it copied)
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+      }
       double v[16];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) v[j] = myslot[j * 128];
+      for (int j = 0; j < 16; ++j) v[j] = myslot[j * jstride];
       uint32_t key = 0;
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
@@ -2894,8 +2944,9 @@ __global__ void __maxnreg__(96)
         key = kj > key ? kj : key;
       }
       smx[(b * 4 + kq) * 128 + r] = key;
-      bool ok = true;
-      if (c >= 2) ok = mbar_wait(sempty0 + 8 * b, (uint32_t)(((c - 2) >> 1) & 1), abort_flag, P.err, 21);
+      bool ok = landed;
+      if (ok && c >= 2)
+        ok = mbar_wait(sempty0 + 8 * b, (uint32_t)(((c - 2) >> 1) & 1), abort_flag, P.err, 21);
       // the four warps of a row group exchange their K quarters' maxima; the
       // groups do not wait for one another, so their latency-bound phases
       // (loads, slicing, TMEM round trips) interleave
@@ -2903,6 +2954,8 @@ __global__ void __maxnreg__(96)
         ok_all = false;
         break;
       }
+      // every warp of the group has its values: the group's box is free
+      if (ao_issuer && c + 1 < nks) issue_box(c + 1);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const uint32_t o = smx[(b * 4 + q) * 128 + r];
@@ -2945,7 +2998,7 @@ __global__ void __maxnreg__(96)
       }
       // the next chunk's copies overlap the previous chunk's epilogue and
       // the next iteration's start (the L2 prefetch keeps their latency short)
-      if (c + 1 < nks) issue_chunk(c + 1);
+      if (!AO_TMA && c + 1 < nks) issue_chunk(c + 1);
       // the previous chunk's epilogue runs while this chunk's MMAs do
       if (c >= 1 && group_any(!epilogue(c - 1), warp & 3)) {
         ok_all = false;
@@ -2953,7 +3006,15 @@ __global__ void __maxnreg__(96)
       }
     }
     // copies still in flight land before the CTA may exit
-    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (AO_TMA) {
+      if (ao_issuer && ao_pending >= 0) {
+        const long long t0 = clock64();
+        while (!mbar_test(aofull, (uint32_t)ao_pending) && clock64() - t0 < WAIT_BUDGET) {
+        }
+      }
+    } else {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+    }
     const bool last_ok = ok_all && epilogue(nks - 1);
     ok_all = !conv_any(!last_ok);  // every converter thread reaches this vote
     if (ok_all) {
@@ -3663,11 +3724,11 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
   int dev = 0, nsm = 0, resident = 0;
   RIMP2_CK(cudaGetDevice(&dev));
   RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 192, smem));
+  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, GEMM_THREADS, smem));
   // persistent CTAs whose TMEM allocations fit an SM together
   resident = std::max(1, std::min(resident, (int)(512 / cols)));
   const long long grid = std::min<long long>(nitems, (long long)nsm * resident);
-  kern<<<(unsigned)grid, 192, smem, s>>>(tA, tB, P);
+  kern<<<(unsigned)grid, GEMM_THREADS, smem, s>>>(tA, tB, P);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;
@@ -3727,13 +3788,31 @@ int ao_half_fused(const double *ao, int NBA, int nbas, const double *Cmo, int no
   P.half = half;
   P.idesc = (1u << 4) | ((uint32_t)(NT >> 3) << 17) | ((uint32_t)(TILE >> 4) << 24);
   P.err = device_error_word();
+  // The AO chunks arrive by TMA (one 16 alpha x 64 nu x 2 mu box per row
+  // group) when the tensor's strides allow it (NBA even: 16-byte multiples)
+  // and its base is 16-byte aligned; otherwise by per-thread cp.async.
+  CUtensorMap tmAO;
+  memset(&tmAO, 0, sizeof tmAO);
+  const bool ao_tma = (NBA % 2 == 0) && ((uintptr_t)ao % 16 == 0);
+  if (ao_tma) {
+    cuuint64_t adims[3] = {(cuuint64_t)NBA, (cuuint64_t)nbas, (cuuint64_t)nbas};
+    cuuint64_t astr[2] = {(cuuint64_t)NBA * 8, (cuuint64_t)NBA * nbas * 8};
+    cuuint32_t abox[3] = {AH_TA, KSTEP, 2};
+    cr = encode(&tmAO, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double *>(ao), adims, astr,
+                abox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) {
+      set_error("cuTensorMapEncodeTiled (AO tensor) failed (%d)", (int)cr);
+      return RIMP2_ERR_CUDA;
+    }
+  }
+  auto kern = ao_tma ? ao_half_kernel<true> : ao_half_kernel<false>;
   const int smem = ah_smem_bytes(NT);
-  RIMP2_CK(cudaFuncSetAttribute(ao_half_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  RIMP2_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   int resident = 0;
-  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, ao_half_kernel, AH_THREADS,
-                                                         smem));
+  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, AH_THREADS, smem));
   if (resident < 1) return RIMP2_OK;  // cannot be resident here: the sliced path runs
-  ao_half_kernel<<<(unsigned)ntiles, AH_THREADS, smem, s>>>(tm, P);
+  kern<<<(unsigned)ntiles, AH_THREADS, smem, s>>>(tm, tmAO, P);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   *handled = true;
