@@ -16,9 +16,13 @@ pair of SMs sharing the B operand, three products, a dummy CTA when an
 occupied index has no partner).  It times both on a grid of occupied
 counts and auxiliary sizes at the bucket's middle virtual count, each shape
 replicated in one graph-launched batch plan until the launch does about
-2 ms of work (CUDA events, best of three), and keeps the thresholds
+2 ms of work (CUDA events, best of three), and fits per-bucket thresholds
 (paired kernel where nocc >= min_nocc and NBA >= min_nba) that minimise the
-summed time over the grid.
+summed time over the grid.  Isolated shapes do not settle it: in a batch
+the two kernels run as separate persistent launches over a mixed queue, so
+the fitted table, uniform tables and "one-CTA kernel only" are then timed
+on a seeded mixed batch of 128 uneven fragments (nocc U[8,64], nvirt
+U[64,512], NBA U[256,2048]) and the fastest table is kept.
 
 The tables are installed in the library with ``apply``
 (rimp2_set_split_buckets, rimp2_set_split_kernel_rule) and can be saved as
@@ -160,8 +164,8 @@ def _fit_rule(grid):
     return best
 
 
-def tune_kernels(buckets, seed=91):
-    """Energy-kernel thresholds for the one-residual-slice buckets."""
+def _grid_rule(buckets, seed):
+    """Per-bucket thresholds fitted to the grid of isolated shapes."""
     rule = []
     for k, b in enumerate(buckets):
         if b["nslices"] != 1:
@@ -188,6 +192,79 @@ def tune_kernels(buckets, seed=91):
     return rule
 
 
+MIX_N, MIX_SEED = 128, 7  # the mixed batch the kernel table is chosen on
+
+
+def mixed_batch_shapes(n=MIX_N, seed=MIX_SEED):
+    """Uneven fragments: nocc ~ U[8,64], nvirt ~ U[64,512], NBA ~ U[256,2048]."""
+    g = np.random.Generator(np.random.Philox(seed))
+    return list(zip(g.integers(8, 65, n).tolist(), g.integers(64, 513, n).tolist(),
+                    g.integers(256, 2049, n).tolist()))
+
+
+def _time_mixed_batch(candidates, seed=123):
+    """Milliseconds per graph launch of one mixed batch under each candidate
+    kernel table (best of three after two warm-up launches)."""
+    import torch
+    st = torch.cuda.Stream()
+    s = st.cuda_stream
+    bufs, desc = [], []
+    with torch.cuda.stream(st):
+        for f, (nocc, nvirt, NBA) in enumerate(mixed_batch_shapes()):
+            d = dict(C=torch.empty(NBA * nvirt * nocc, dtype=torch.float64, device="cuda"),
+                     eo=torch.empty(nocc, dtype=torch.float64, device="cuda"),
+                     ev=torch.empty(nvirt, dtype=torch.float64, device="cuda"),
+                     E=torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda"),
+                     T=torch.zeros(1, dtype=torch.float64, device="cuda"))
+            api.gen_fragment_dev(seed + f, nocc, nvirt, NBA, d["C"].data_ptr(), d["eo"].data_ptr(),
+                                 d["ev"].data_ptr(), stream=s)
+            bufs.append(d)
+            desc.append((nocc, nvirt, NBA, d["C"].data_ptr(), d["eo"].data_ptr(),
+                         d["ev"].data_ptr(), d["E"].data_ptr(), d["T"].data_ptr()))
+    st.synchronize()
+    out = {}
+    for name, table in candidates.items():
+        api.set_split_kernel_rule([x["nvirt_min"] for x in table], [x["min_nocc"] for x in table],
+                                  [x["min_nba"] for x in table])
+        plan = api.BatchPlan(desc, graph=True, stream=s)
+        for _ in range(2):
+            plan.execute(stream=s)
+        best = float("inf")
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            plan.execute(stream=s)
+            e1.record(st)
+            st.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        api.sync_status(s)
+        plan.close()
+        out[name] = best
+    return out
+
+
+def tune_kernels(buckets, seed=91):
+    """Energy-kernel table for the one-residual-slice buckets: thresholds
+    fitted per bucket to isolated shapes, then that table and uniform
+    tables timed on a mixed batch of uneven fragments, whose graph-launched
+    persistent groups are what a batch runs; the fastest table is kept."""
+    grid = _grid_rule(buckets, seed)
+    strip = lambda t: [{k: x[k] for k in ("nvirt_min", "min_nocc", "min_nba")} for x in t]  # noqa: E731
+    cands = {"grid_fit": strip(grid), "one_cta_only": [dict(nvirt_min=0, min_nocc=NEVER,
+                                                           min_nba=NEVER)]}
+    for mo in (8, 10, 16, 24):
+        for mb in (512, 1024, 1536):
+            cands[f"nocc>={mo},NBA>={mb}"] = [dict(nvirt_min=0, min_nocc=mo, min_nba=mb)]
+    times = _time_mixed_batch(cands)
+    best = min(times, key=times.get)
+    table = [dict(x, chosen_by=best) for x in cands[best]]
+    return table, {"chosen": best, "mixed_batch": {"fragments": MIX_N, "seed": MIX_SEED,
+                                                     "shapes": "nocc U[8,64], nvirt U[64,512], "
+                                                               "NBA U[256,2048]"},
+                   "batch_ms": times, "grid_fit": grid}
+
+
 def tune(seed=77):
     table = []
     for k, lo in enumerate(BUCKET_EDGES):
@@ -208,8 +285,9 @@ def tune(seed=77):
                      "FP32-accumulated correction against; the library also sends every "
                      "fragment with nocc*nvirt < 64 to FP64 (its FP32 epilogue rounding "
                      "leaves 2-5e-8 on such pair energies)"}
+    rule, sel = tune_kernels(table)
     return {"target": TARGET, "margin": 0.5, "buckets": [fixed] + table,
-            "kernel_rule": tune_kernels(table)}
+            "kernel_rule": rule, "kernel_rule_selection": sel}
 
 
 def apply(table):
@@ -237,7 +315,9 @@ def main():
     if a.kernels_only:
         with open(a.kernels_only) as f:
             t = json.load(f)
-        t["kernel_rule"] = tune_kernels([x for x in t["buckets"] if x["nvirt_min"] > 0])
+        apply(t)  # the slice counts the batch runs with
+        t["kernel_rule"], t["kernel_rule_selection"] = tune_kernels(
+            [x for x in t["buckets"] if x["nvirt_min"] > 0])
     else:
         t = tune()
     apply(t)

@@ -1003,14 +1003,15 @@ int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices) {
 // <= nvirt), else the one-CTA kernel (128-row tiles, four products).  The
 // paired kernel's per-item costs (the exchange-tile transpose, cross-CTA
 // hand-offs, a dummy CTA for an odd count of i <= j) lose on short auxiliary
-// spaces and few occupied orbitals.  Default = the thresholds measured by
+// spaces and few occupied orbitals.  Default = the table chosen by
 // rimp2_gpu_gb300/autotune.py on GB300 (rimp2_gpu_gb300/tuning/
-// split_buckets.json, "kernel_rule"); rimp2_set_split_kernel_rule replaces it.
+// split_buckets.json, "kernel_rule": fitted per bucket on isolated shapes,
+// then selected among candidate tables on a mixed batch, where one uniform
+// table matched the per-bucket fit); rimp2_set_split_kernel_rule replaces it.
 struct KernelRule {
   int nvirt_min, min_nocc, min_nba;
 };
-static std::vector<KernelRule> g_krule = {{0, 32, 1024}, {192, 32, 1024}, {256, 16, 2048},
-                                           {384, 16, 1024}};
+static std::vector<KernelRule> g_krule = {{0, 16, 512}};
 
 }  // extern "C"
 

@@ -2339,11 +2339,8 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
 // tiles.  Per K16 step one MMA over the stacked B planes [S0b; R1b] (N = 2 NT)
 // gives L0 and S0a R1b, then R1a S0b, R1a R1b (and S0a R2b, R2a S0b with two
 // residual slices) accumulate into L1.
-// Roles: warp 0 TMA producer, warp 1 MMA issuer and TMEM owner, warps 2-9
-// epilogue (two per TMEM lane quadrant, alternate 16-column chunks).  The
-// epilogue scales L0 and L1 by the row and column powers of two in FP32
-// (exact) and adds them once in FP64: GB300's FP64 pipe is slow, and it
-// bounds this kernel's epilogue.  Every wait is bounded.
+// Roles: warp 0 TMA producer, warp 1 MMA issuer and TMEM owner, warps 2-5
+// epilogue (one per TMEM lane quadrant).  Every wait is bounded.
 // ==========================================================================
 struct GemmSP {
   int M, N, NT, nks, mtiles, ntiles, nbatch;
@@ -2363,10 +2360,8 @@ constexpr int gemm_smem_bytes(int nsl, int NT) {
   return GEMM_NST * gemm_stage_bytes(nsl, NT) + 1024 + 256;
 }
 
-constexpr int GEMM_THREADS = 64 + 32 * 8;
-
 template <int NSL>
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
+__global__ void __launch_bounds__(192, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       GemmSP P) {
   constexpr int NST = GEMM_NST;
@@ -2392,7 +2387,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     }
     for (int u = 0; u < 2; ++u) {
       mbar_init(tfull0 + 8 * u, 1);
-      mbar_init(tempty0 + 8 * u, 8);  // the eight epilogue warps
+      mbar_init(tempty0 + 8 * u, 4);  // the four epilogue warps
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -2520,7 +2515,6 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   } else {
     // ------------------------------ epilogue ----------------------------------
     const int quad = warp & 3;
-    const int half = (warp - 2) >> 2;  // 16-column chunks half, half + 2, ...
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     long long t = 0;
@@ -2532,10 +2526,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       int b, mt, nt;
       tile_rows(item, arow, brow, b, mt, nt);
       const long long m = (long long)mt * TILE + row;
-      const float sa = P.a_inv[arow + row];
+      const double sa = (double)P.a_inv[arow + row];
       const uint32_t taddr = tmem + lane_off + (uint32_t)(u * 2 * NT);
       double *orow = P.out + (long long)b * P.sOb + m * P.sOm;
-      for (int c0 = 16 * half; c0 < NT; c0 += 32) {
+      for (int c0 = 0; c0 < NT; c0 += 16) {
         float l0[16], l1[16];
         tmem_ld16(taddr + c0, l0);
         tmem_ld16(taddr + NT + c0, l1);
@@ -2545,17 +2539,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           for (int k = 0; k < 16; ++k) {
             const int n = nt * NT + c0 + k;
             if (n < P.N) {
-              const float sb = P.b_inv[brow + c0 + k];
-              const float sc = sa * sb;  // a power of two
-              double v;
-              if (sc >= 0x1p-100f) {
-                // l0 (an integer below 2^24) and l1 times sc are exact
-                // floats; one FP64 addition, rounded as (l0 + l1) sc
-                v = (double)(l0[k] * sc) + (double)(l1[k] * sc);
-              } else {  // scales too small for FP32: the same sum in FP64
-                v = ((double)l0[k] + (double)l1[k]) * ((double)sa * (double)sb);
-              }
-              orow[(long long)n * P.sOn] = v;
+              const double sb = (double)P.b_inv[brow + c0 + k];
+              orow[(long long)n * P.sOn] = ((double)l0[k] + (double)l1[k]) * (sa * sb);
             }
           }
         }
@@ -3724,11 +3709,11 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
   int dev = 0, nsm = 0, resident = 0;
   RIMP2_CK(cudaGetDevice(&dev));
   RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, GEMM_THREADS, smem));
+  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 192, smem));
   // persistent CTAs whose TMEM allocations fit an SM together
   resident = std::max(1, std::min(resident, (int)(512 / cols)));
   const long long grid = std::min<long long>(nitems, (long long)nsm * resident);
-  kern<<<(unsigned)grid, GEMM_THREADS, smem, s>>>(tA, tB, P);
+  kern<<<(unsigned)grid, 192, smem, s>>>(tA, tB, P);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;

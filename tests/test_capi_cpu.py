@@ -282,9 +282,11 @@ def test_tuned_tables_match_library_defaults():
             "for b in t['buckets']:\n"
             "    assert api.split_nslices(max(b['nvirt_min'], 64), 4, 64) == b['nslices'] or "
             "b['nvirt_min'] < 16, b\n"
-            "for r in t.get('kernel_rule', []):\n"
-            "    if r['nvirt_min'] == 0: continue\n"
-            "    nv = r['nvirt_min']\n"
+            "rules = t.get('kernel_rule', [])\n"
+            "for k, r in enumerate(rules):\n"
+            "    if r['nvirt_min'] == 0 and len(rules) > 1: continue\n"
+            "    nv = max(r['nvirt_min'], 192)\n"
+            "    if k + 1 < len(rules) and nv >= rules[k + 1]['nvirt_min']: continue\n"
             "    if api.split_nslices(nv, 64, 4096) != 1: continue\n"
             "    mo, mb = r['min_nocc'], r['min_nba']\n"
             "    if mo < 65536 and mb < 65536:\n"
