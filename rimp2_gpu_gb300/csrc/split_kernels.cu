@@ -325,6 +325,35 @@ __device__ __forceinline__ float abs_trunc_f32(unsigned long long mag) {
   return __uint_as_float((unsigned int)((mag >> 29) - (896ull << 23)));
 }
 
+// Split of a double x with |x 2^e| < 2^22 into q (an integer, rounded half to
+// even; |q| <= 512 for the AO chunks, <= 2048 for Calpha columns) and r ~ x 2^e - q in FP32 arithmetic only (GB300's
+// FP64 pipe is a small fraction of the FP32 one): v = |x| 2^e is the float
+// f_hi holding the top 24 significant bits of x (exponent and fraction bits
+// moved into place, no rounding) plus f_lo holding the next 23 bits (a 23-bit
+// integer formed with the 2^23 magic constant, times a power of two);
+// q = round(f_hi) with the 1.5 * 2^23 constant, r = (f_hi - q) + f_lo, where
+// f_hi - q is exact and the sum rounds once (2^-25 of |r|).  Values below
+// 2^-40 of the scaled unit, zeros and subnormals give q = r = 0.  The sign
+// of x goes onto both.  Equal to split_int's results to within its rounding
+// of r (checked by emulation of these float operations against exact
+// rational arithmetic).
+__device__ __forceinline__ void split_f32(double x, int e, float &q, float &r) {
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  const uint32_t sgn = hi & 0x80000000u;
+  const int ed = (int)((hi >> 20) & 0x7FFu);
+  const int E = ed - 1023 + e;  // |x| 2^e = 1.f 2^E
+  const bool live = ed != 0 && E >= -40;
+  const int Ec = live ? E : 0;
+  const uint32_t frac23 = (__funnelshift_l(lo, hi, 3)) & 0x7FFFFFu;
+  const float fhi = __uint_as_float(((uint32_t)(Ec + 127) << 23) | frac23);
+  const float lo23 = __uint_as_float(0x4B000000u | ((lo >> 6) & 0x7FFFFFu)) - 8388608.0f;
+  const float flo = lo23 * __uint_as_float((uint32_t)(Ec - 46 + 127) << 23);
+  const float qm = (fhi + 12582912.0f) - 12582912.0f;
+  const float rm = (fhi - qm) + flo;
+  q = live ? __uint_as_float(__float_as_uint(qm) | sgn) : 0.0f;
+  r = live ? __uint_as_float(__float_as_uint(rm) ^ sgn) : 0.0f;
+}
+
 // x = |v| 2^e split into q = rint(x) (round half to even; |q| <= 2048 by the
 // choice of e) and the remainder r = x - q, from A = floor(x 2^32): the
 // integer part and the 32 bits below it of the 53-bit mantissa.  r is exact
@@ -395,9 +424,10 @@ __global__ void __launch_bounds__(256, 6)
   __half *out = slices + (size_t)(F.row_base + col) * 64;
   const size_t kstride = (size_t)F.ncol * 64;  // next K chunk of the same column
   if (a >= F.nvirt) {
-    for (int k = lane; k < Kpad; k += 32) {
-      const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
-      for (int sl = 0; sl < nsl + vplane; ++sl) out[sl * plane + o] = hz;
+    for (int k0 = 4 * lane; k0 < Kpad; k0 += 128) {
+      const size_t o = (size_t)(k0 >> 6) * kstride + (k0 & 63);
+      for (int sl = 0; sl < nsl + vplane; ++sl)
+        *reinterpret_cast<uint2 *>(out + sl * plane + o) = make_uint2(0u, 0u);
     }
     if (lane == 0) {
       inv_scale[F.col_base + col] = 1.0f;
@@ -435,36 +465,37 @@ __global__ void __launch_bounds__(256, 6)
   for (int attempt = 0; attempt < 64; ++attempt) {
     long long n2 = 0;  // sum of S0^2 (integers; <= 2^24 is the test)
     float dsum = 0.0f;  // sum of R1 (V - S0 - R1) (V plane only)
-    for (int k0 = lane; k0 < Kpad; k0 += 128) {
+    // four consecutive K values per lane (one 8-byte store per plane; a
+    // 64-wide K chunk holds 16 lanes' groups); values beyond NBA are zeros
+    for (int k0 = 4 * lane; k0 < Kpad; k0 += 128) {
       double v[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = (k0 + 32 * u < NBA) ? c[k0 + 32 * u] : 0.0;
+      for (int u = 0; u < 4; ++u) v[u] = (k0 + u < NBA) ? c[k0 + u] : 0.0;
+      __align__(8) __half h0[4], h1[4], h2[4], hv[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int k = k0 + 32 * u;
-        if (k >= Kpad) break;
-        __half h0 = hz, h1 = hz, h2 = hz, hv = hz;
-        if (k < NBA) {
-          float q, r;
-          split_int((unsigned long long)__double_as_longlong(v[u]), e, q, r);
-          h0 = __float2half_rn(q);  // integer |q| <= 2048: exact in FP16
-          h1 = __float2half_rn(r);
-          h2 = __float2half_rn(r - __half2float(h1));
-          const int qi = (int)q;
-          n2 += qi * qi;  // |q| <= 2048: q^2 fits an int
-          if (vplane) {
-            // V = C*s in FP16; its rounding error against S0 + R1 is exact in FP32
-            hv = __float2half_rn(q + r);
-            const float r1 = __half2float(h1);
-            dsum = fmaf(r1, (__half2float(hv) - q) - r1, dsum);
-          }
+        float q, r;
+        split_f32(v[u], e, q, r);  // zeros give q = r = 0
+        h0[u] = __float2half_rn(q);  // integer |q| <= 2048: exact in FP16
+        h1[u] = __float2half_rn(r);
+        h2[u] = __float2half_rn(r - __half2float(h1[u]));
+        // |q| < 2^23: its integer value from the 2^23 magic constant
+        const int qi = __float_as_int(fabsf(q) + 8388608.0f) - 0x4B000000;
+        n2 += qi * qi;  // |q| <= 2048: q^2 fits an int
+        if (vplane) {
+          // V = C*s in FP16; its rounding error against S0 + R1 is exact in FP32
+          hv[u] = __float2half_rn(q + r);
+          const float r1 = __half2float(h1[u]);
+          dsum = fmaf(r1, (__half2float(hv[u]) - q) - r1, dsum);
         }
-        const size_t o = (size_t)(k >> 6) * kstride + (k & 63);
-        out[o] = h0;
-        if (nsl > 1) out[plane + o] = h1;
-        if (nsl > 2) out[2 * plane + o] = h2;
-        if (vplane) out[nsl * plane + o] = hv;
       }
+      const size_t o = (size_t)(k0 >> 6) * kstride + (k0 & 63);
+      *reinterpret_cast<uint2 *>(out + o) = *reinterpret_cast<const uint2 *>(h0);
+      if (nsl > 1) *reinterpret_cast<uint2 *>(out + plane + o) = *reinterpret_cast<const uint2 *>(h1);
+      if (nsl > 2)
+        *reinterpret_cast<uint2 *>(out + 2 * plane + o) = *reinterpret_cast<const uint2 *>(h2);
+      if (vplane)
+        *reinterpret_cast<uint2 *>(out + nsl * plane + o) = *reinterpret_cast<const uint2 *>(hv);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
@@ -2649,33 +2680,85 @@ __device__ __forceinline__ void tmem_wait_st() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-// Split of a double x with |x 2^e| <= 511.5 into q (an integer, |q| <= 512,
-// rounded half to even) and r ~ x 2^e - q in FP32 arithmetic only (GB300's
-// FP64 pipe is a small fraction of the FP32 one): v = |x| 2^e is the float
-// f_hi holding the top 24 significant bits of x (exponent and fraction bits
-// moved into place, no rounding) plus f_lo holding the next 23 bits (a 23-bit
-// integer formed with the 2^23 magic constant, times a power of two);
-// q = round(f_hi) with the 1.5 * 2^23 constant, r = (f_hi - q) + f_lo, where
-// f_hi - q is exact and the sum rounds once (2^-25 of |r|).  Values below
-// 2^-40 of the scaled unit, zeros and subnormals give q = r = 0.  The sign
-// of x goes onto both.  Equal to split_int's results to within its rounding
-// of r (checked by emulation of these float operations against exact
-// rational arithmetic).
-__device__ __forceinline__ void split_f32(double x, int e, float &q, float &r) {
-  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-  const uint32_t sgn = hi & 0x80000000u;
-  const int ed = (int)((hi >> 20) & 0x7FFu);
-  const int E = ed - 1023 + e;  // |x| 2^e = 1.f 2^E
-  const bool live = ed != 0 && E >= -40;
-  const int Ec = live ? E : 0;
-  const uint32_t frac23 = (__funnelshift_l(lo, hi, 3)) & 0x7FFFFFu;
-  const float fhi = __uint_as_float(((uint32_t)(Ec + 127) << 23) | frac23);
-  const float lo23 = __uint_as_float(0x4B000000u | ((lo >> 6) & 0x7FFFFFu)) - 8388608.0f;
-  const float flo = lo23 * __uint_as_float((uint32_t)(Ec - 46 + 127) << 23);
-  const float qm = (fhi + 12582912.0f) - 12582912.0f;
-  const float rm = (fhi - qm) + flo;
-  q = live ? __uint_as_float(__float_as_uint(qm) | sgn) : 0.0f;
-  r = live ? __uint_as_float(__float_as_uint(rm) ^ sgn) : 0.0f;
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+
+// Fold of W columns (4 or 8) of one AO chunk's products into the running
+// double-float totals: L0 and L1 scaled by the row and column powers of two
+// (exact), added to hi/lo with a two-sum of the high parts (first chunk:
+// assigned), written back to TMEM -- or, on the last chunk, turned into
+// FP64 in the staging area ([column][alpha][mu], 9-double pitch per alpha).
+template <int W>
+__device__ __forceinline__ void ah_fold(uint32_t tL0, int NT, uint32_t rs_hi, uint32_t rs_lo,
+                                        int col, float sa, const float *sbc, bool first,
+                                        bool last, double *stg, int a_l, int m_l) {
+  float l0[W], l1[W], hi[W], lo[W], sbk[W];
+#pragma unroll
+  for (int q = 0; q < W; q += 4) {  // 16-byte loads (NT and col are multiples of 4)
+    const float4 sb4 = *reinterpret_cast<const float4 *>(sbc + col + q);
+    sbk[q] = sb4.x;
+    sbk[q + 1] = sb4.y;
+    sbk[q + 2] = sb4.z;
+    sbk[q + 3] = sb4.w;
+  }
+  if constexpr (W == 8) {
+    tmem_ld8(tL0 + col, l0);
+    tmem_ld8(tL0 + NT + col, l1);
+    if (!first) {
+      tmem_ld8(rs_hi + col, hi);
+      tmem_ld8(rs_lo + col, lo);
+    }
+  } else {
+    tmem_ld4(tL0 + col, l0);
+    tmem_ld4(tL0 + NT + col, l1);
+    if (!first) {
+      tmem_ld4(rs_hi + col, hi);
+      tmem_ld4(rs_lo + col, lo);
+    }
+  }
+  tmem_wait_ld();
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    const float sc = sa * sbk[k];  // power of two: the products below are exact
+    const float xh = l0[k] * sc, xl = l1[k] * sc;
+    if (first) {
+      hi[k] = xh;
+      lo[k] = xl;
+    } else {  // two-sum of the high parts, low parts added
+      const float s = hi[k] + xh;
+      const float bv = s - hi[k];
+      const float err = (hi[k] - (s - bv)) + (xh - bv);
+      lo[k] = lo[k] + xl + err;
+      hi[k] = s;
+    }
+  }
+  if (!last) {
+    if constexpr (W == 8) {
+      tmem_st8(rs_hi + col, hi);
+      tmem_st8(rs_lo + col, lo);
+    } else {
+      tmem_st4(rs_hi + col, hi);
+      tmem_st4(rs_lo + col, lo);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < W; ++k) stg[(col + k) * AH_STG + a_l * 9 + m_l] = (double)hi[k] + (double)lo[k];
+  }
 }
 
 // Exponent e with |x| 2^e <= 511.5 (to within 2^-11) for the largest
@@ -2856,44 +2939,12 @@ __global__ void __maxnreg__(96)
       const float *sbc = P.sb + (size_t)ce * NT;
       const bool last = ce + 1 == nks;
       double *stg = reinterpret_cast<double *>(stages);
-      for (int col = col0; col < col0 + ncol; col += 4) {
-        float l0[4], l1[4], hi[4], lo[4];
-        // the four column scales of the chunk in one 16-byte load (NT and
-        // col are multiples of 4)
-        const float4 sb4 = *reinterpret_cast<const float4 *>(sbc + col);
-        const float sbk[4] = {sb4.x, sb4.y, sb4.z, sb4.w};
-        tmem_ld4(tL0 + col, l0);
-        tmem_ld4(tL0 + NT + col, l1);
-        if (ce > 0) {
-          tmem_ld4(rs_hi + col, hi);
-          tmem_ld4(rs_lo + col, lo);
-        }
-        tmem_wait_ld();
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const float sc = sa * sbk[k];  // power of two: the products below are exact
-          const float xh = l0[k] * sc, xl = l1[k] * sc;
-          if (ce == 0) {
-            hi[k] = xh;
-            lo[k] = xl;
-          } else {  // two-sum of the high parts, low parts added
-            const float s = hi[k] + xh;
-            const float bv = s - hi[k];
-            const float err = (hi[k] - (s - bv)) + (xh - bv);
-            lo[k] = lo[k] + xl + err;
-            hi[k] = s;
-          }
-        }
-        if (!last) {
-          tmem_st4(rs_hi + col, hi);
-          tmem_st4(rs_lo + col, lo);
-        } else {
-          // [column][alpha][mu] with a 9-double pitch per alpha
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            stg[(col + k) * AH_STG + a_l * 9 + m_l] = (double)hi[k] + (double)lo[k];
-        }
-      }
+      // eight columns per TMEM round trip, four for a remainder
+      int col = col0;
+      for (; col + 8 <= col0 + ncol; col += 8)
+        ah_fold<8>(tL0, NT, rs_hi, rs_lo, col, sa, sbc, ce == 0, last, stg, a_l, m_l);
+      if (col < col0 + ncol)
+        ah_fold<4>(tL0, NT, rs_hi, rs_lo, col, sa, sbc, ce == 0, last, stg, a_l, m_l);
       if (!last) tmem_wait_st();
       tc_fence_before();
       __syncwarp();
