@@ -335,8 +335,8 @@ __device__ __forceinline__ float abs_trunc_f32(unsigned long long mag) {
 // f_hi - q is exact and the sum rounds once (2^-25 of |r|).  Values below
 // 2^-40 of the scaled unit, zeros and subnormals give q = r = 0.  The sign
 // of x goes onto both.  Equal to split_int's results to within its rounding
-// of r (checked by emulation of these float operations against exact
-// rational arithmetic).
+// of r; tests/test_split_numerics_cpu.py restates these float operations and
+// checks them against exact rational arithmetic.
 __device__ __forceinline__ void split_f32(double x, int e, float &q, float &r) {
   const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
   const uint32_t sgn = hi & 0x80000000u;

@@ -67,3 +67,51 @@ def test_three_product_form_with_diagonal_correction():
     # the correction removes most of the i=j bias and lands near the exact form
     assert diag_bias["3c"] < 0.6 * diag_bias["3"]
     assert worst["3c"] <= 1.5 * worst["4"] + 5e-9
+
+
+def _f32(bits):
+    return np.array([bits], dtype=np.uint32).view(np.float32)[0]
+
+
+def split_f32_emulated(x, e):
+    """The device split of a double x with |x 2^e| < 2^22 (split_f32 in
+    split_kernels.cu) restated step by step in numpy float32: f_hi from the
+    top 24 significant bits (bit moves only), f_lo from the next 23 bits via
+    the 2^23 magic constant, q = round(f_hi) via 1.5 * 2^23, r = (f_hi - q)
+    + f_lo, the sign of x applied to both; below 2^-40 of the scaled unit,
+    zeros and subnormals give q = r = 0."""
+    b = int(np.array([x], dtype=np.float64).view(np.uint64)[0])
+    hi, lo = b >> 32, b & 0xFFFFFFFF
+    sgn = hi & 0x80000000
+    ed = (hi >> 20) & 0x7FF
+    E = ed - 1023 + e
+    if ed == 0 or E < -40:
+        return np.float32(0.0), np.float32(0.0)
+    frac23 = ((hi << 3) | (lo >> 29)) & 0x7FFFFF
+    fhi = _f32(((E + 127) << 23) | frac23)
+    lo23 = np.float32(_f32(0x4B000000 | ((lo >> 6) & 0x7FFFFF)) - np.float32(8388608.0))
+    flo = np.float32(lo23 * _f32((E - 46 + 127) << 23))
+    qm = np.float32(np.float32(fhi + np.float32(12582912.0)) - np.float32(12582912.0))
+    rm = np.float32(np.float32(fhi - qm) + flo)
+    return (-qm, -rm) if sgn else (qm, rm)
+
+
+def test_fp32_split_of_doubles_against_exact_arithmetic():
+    """q is an integer within the bound, q + r equals x 2^e to 2^-25 of |r|
+    plus the 2^-37 dropped below f_lo (checked in exact rationals), and
+    |r| <= 1/2 whenever |x 2^e| >= 1 (round half to even)."""
+    from fractions import Fraction
+    rng = np.random.default_rng(3)
+    for bound in (511.5, 2047.5):
+        for _ in range(4000):
+            e = int(rng.integers(-60, 60))
+            mag = float(rng.choice([rng.uniform(0, bound), 10 ** rng.uniform(-14, np.log10(bound)),
+                                    bound, 0.5, 1.5, 2.5]))
+            x = np.ldexp(min(mag, bound), -e) * (1 if rng.random() < 0.5 else -1)
+            q, r = split_f32_emulated(x, e)
+            v = Fraction(float(x)) * Fraction(2) ** e
+            assert float(q) == int(q) and abs(q) <= bound + 0.5
+            err = abs(Fraction(float(q)) + Fraction(float(r)) - v)
+            assert err <= Fraction(abs(float(r))) * Fraction(1, 2 ** 24) + Fraction(1, 2 ** 36)
+            if abs(v) >= 1:
+                assert abs(Fraction(float(r))) <= Fraction(1, 2) + Fraction(1, 2 ** 20)
