@@ -325,6 +325,27 @@ __device__ __forceinline__ float abs_trunc_f32(unsigned long long mag) {
   return __uint_as_float((unsigned int)((mag >> 29) - (896ull << 23)));
 }
 
+// float -> double by moving bits (GB300 runs the F2F conversion on its slow
+// FP64 pipe): normal floats and zero; a subnormal float becomes zero.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t ex = (u >> 23) & 0xFFu;
+  const uint32_t hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u >> 3) & 0xFFFFFu);
+  const uint32_t lo = u << 29;
+  return ex == 0 ? 0.0 : __hiloint2double((int)hi, (int)lo);
+}
+
+// v * p for p = 2^k (a normal float) by adding k to v's exponent field:
+// exact; zero stays zero, a result below the normal range becomes zero.
+__device__ __forceinline__ double scale_pow2(double v, float p) {
+  const int k = (int)((__float_as_uint(p) >> 23) & 0xFFu) - 127;
+  const long long bits = __double_as_longlong(v);
+  const int ev = (int)((bits >> 52) & 0x7FF);
+  if (ev == 0) return v;
+  if (ev + k <= 0) return 0.0;
+  return __longlong_as_double(bits + ((long long)k << 52));
+}
+
 // Split of a double x with |x 2^e| < 2^22 into q (an integer, rounded half to
 // even; |q| <= 512 for the AO chunks, <= 2048 for Calpha columns) and r ~ x 2^e - q in FP32 arithmetic only (GB300's
 // FP64 pipe is a small fraction of the FP32 one): v = |x| 2^e is the float
@@ -2386,6 +2407,7 @@ struct GemmSP {
 };
 
 constexpr int GEMM_NST = 2;
+
 constexpr int gemm_stage_bytes(int nsl, int NT) { return nsl * (PANEL_BYTES + NT * 128); }
 constexpr int gemm_smem_bytes(int nsl, int NT) {
   return GEMM_NST * gemm_stage_bytes(nsl, NT) + 1024 + 256;
@@ -2557,7 +2579,7 @@ __global__ void __launch_bounds__(192, 1)
       int b, mt, nt;
       tile_rows(item, arow, brow, b, mt, nt);
       const long long m = (long long)mt * TILE + row;
-      const double sa = (double)P.a_inv[arow + row];
+      const float sa = P.a_inv[arow + row];  // 2^-e of this row
       const uint32_t taddr = tmem + lane_off + (uint32_t)(u * 2 * NT);
       double *orow = P.out + (long long)b * P.sOb + m * P.sOm;
       for (int c0 = 0; c0 < NT; c0 += 16) {
@@ -2570,8 +2592,15 @@ __global__ void __launch_bounds__(192, 1)
           for (int k = 0; k < 16; ++k) {
             const int n = nt * NT + c0 + k;
             if (n < P.N) {
-              const double sb = (double)P.b_inv[brow + c0 + k];
-              orow[(long long)n * P.sOn] = ((double)l0[k] + (double)l1[k]) * (sa * sb);
+              // (L0 + L1) sa sb with one FP64 operation: L0 (an integer
+              // below 2^24) and L1 times the row's power of two are exact
+              // floats (|L1 sa| below 2^-126, far under the output's
+              // resolution, flushes), their sum rounds once in FP64 as
+              // (L0 + L1) does, and the column's power of two moves the
+              // exponent.  The FP64 pipe, not the tensor core, bounded this
+              // epilogue with FP64 conversions and products per element.
+              const double v = f2d_bits(l0[k] * sa) + f2d_bits(l1[k] * sa);
+              orow[(long long)n * P.sOn] = scale_pow2(v, P.b_inv[brow + c0 + k]);
             }
           }
         }
@@ -2757,7 +2786,8 @@ __device__ __forceinline__ void ah_fold(uint32_t tL0, int NT, uint32_t rs_hi, ui
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < W; ++k) stg[(col + k) * AH_STG + a_l * 9 + m_l] = (double)hi[k] + (double)lo[k];
+    for (int k = 0; k < W; ++k)  // one FP64 add per output (bit-moved conversions)
+      stg[(col + k) * AH_STG + a_l * 9 + m_l] = f2d_bits(hi[k]) + f2d_bits(lo[k]);
   }
 }
 
