@@ -3209,7 +3209,10 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
   const size_t kstride = (size_t)nrows_pad * 64;
   if (blockIdx.x == 0 && blockIdx.y == 0)
     for (long long t = MK + threadIdx.x; t < nrows_pad; t += blockDim.x) inv_scale[t] = 1.0f;
-  const double *src = ao + (live ? al + (size_t)NBA * mu : 0);  // element nu at src[MK*nu]
+  // row (alpha, mu) over K = nu read along the middle index: (alpha|mu nu) =
+  // (alpha|nu mu), 8 NBA bytes apart, so a row's values stay within a few
+  // memory pages (along the last index they are 8 NBA nbas bytes apart)
+  const double *src = ao + (live ? al + (size_t)MK * mu : 0);  // element nu at src[NBA*nu]
   int e = 0;
   if (live) {
     unsigned long long mxb = 0;
@@ -3219,7 +3222,7 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
     for (int nu0 = 0; nu0 < nbas; nu0 += 16) {
       double v[16];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) v[q] = (nu0 + q < nbas) ? src[(size_t)MK * (nu0 + q)] : 0.0;
+      for (int q = 0; q < 16; ++q) v[q] = (nu0 + q < nbas) ? src[(size_t)NBA * (nu0 + q)] : 0.0;
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
         const unsigned long long mag =
@@ -3248,7 +3251,7 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           const int nu = kc * 64 + q00 + q;
-          v[q] = (live && nu < nbas) ? src[(size_t)MK * nu] : 0.0;
+          v[q] = (live && nu < nbas) ? src[(size_t)NBA * nu] : 0.0;
         }
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
@@ -3259,11 +3262,11 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
             h0[q] = h1[q] = h2[q] = hz;
             if (live && nu < nbas) {
               float qv, r;
-              split_int((unsigned long long)__double_as_longlong(v[8 * hh + q]), e, qv, r);
+              split_f32(v[8 * hh + q], e, qv, r);  // |x 2^e| <= 2047.5
               h0[q] = __float2half_rn(qv);
               h1[q] = __float2half_rn(r);
               h2[q] = __float2half_rn(r - __half2float(h1[q]));
-              const int qi = (int)qv;
+              const int qi = __float_as_int(fabsf(qv) + 8388608.0f) - 0x4B000000;
               n2 += qi * qi;
             }
           }
