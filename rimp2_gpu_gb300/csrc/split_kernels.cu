@@ -2156,24 +2156,19 @@ cudaError_t launch_hi(void (*k)(KArgs...), unsigned grid, unsigned block, size_t
 }
 
 // Stage count of the paired kernel for a group.  The fourth 56 KB stage
-// (which needs the exchange tile transposed through global scratch instead of
-// shared memory) covers the cross-CTA refill round trip on long product
-// chains; on short ones the per-item epilogue is exposed and the slower
-// global-memory transpose costs more than the deeper ring gains.  Decided on
-// the work-weighted mean of the group's K chunks; RIMP2_PAIR_STAGES=3 or =4
-// in the environment overrides it.
+// (which needs the exchange tile transposed through global scratch instead
+// of shared memory) covers the cross-CTA refill round trip on long product
+// chains, but measured on GB300 it gains nothing where it matters: the
+// nocc=128 nvirt=1024 NBA=4096 fragment takes 5% fewer cycles at the same
+// time (the power cap lowers the clock), and the 256-fragment batch runs 6%
+// slower (569-572 against 605-608 eff TFLOP/s, same box: the slower
+// global-memory transpose is exposed on short items).  So three stages;
+// RIMP2_PAIR_STAGES=4 in the environment selects the four-stage form.
 int pair_stages_for(const std::vector<FragDesc> &fh) {
+  (void)fh;
   const char *e = getenv("RIMP2_PAIR_STAGES");
-  if (e && e[0] == '3') return 3;
   if (e && e[0] == '4') return 4;
-  double w = 0.0, wk = 0.0;
-  for (const auto &F : fh) {
-    const double work = (double)pair_items_before(F.nocc) * F.ntp * F.nks;
-    w += work;
-    wk += work * F.nks;
-  }
-  (void)wk;
-  return 3;  // the four-stage form is opt-in until measured
+  return 3;
 }
 
 int launch_pair(const Group &g, PairParams Q, int npair, cudaStream_t s) {
