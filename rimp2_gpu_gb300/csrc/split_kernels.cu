@@ -2624,9 +2624,11 @@ __global__ void __launch_bounds__(192, 1)
 // page (the last index is 8 NBA nbas bytes apart: a chunk would touch 64).
 // GEMM rows are (alpha, mu) -- 16 alpha x 8 mu per CTA tile, row r = a + 16 m
 // -- K = nu in chunks of 64, N = the occupied orbitals (NT <= 80, padded to
-// a multiple of 16).  The AO tensor is read once, by converter warps, with
-// coalesced loads (16 consecutive alpha of two mu rows per warp load), and
-// sliced in shared memory with a power-of-two scale per (row, K chunk):
+// a multiple of 16).  The AO tensor is read once -- per row group (the 32
+// rows of 16 alpha x 2 mu) one 16 alpha x 64 nu x 2 mu TMA box per chunk
+// (even NBA, 16-byte aligned tensor), or per-thread 8-byte cp.async copies
+// otherwise -- and sliced by the converter warps (an FP32-arithmetic split,
+// split_f32) with a power-of-two scale per (row, K chunk):
 // |x 2^e| <= 511.5, so S0 is a 10-bit integer, and with the occupied MO
 // block sliced the same way (per column and chunk, precomputed) every
 // partial sum of S0a S0b over a chunk is below 64 * 511^2 < 2^24: the integer
@@ -2636,22 +2638,24 @@ __global__ void __launch_bounds__(192, 1)
 // column scales of that chunk (powers of two: exact) and adds them into a
 // double-float (FP32 hi + lo, two-sum) running total kept in TMEM, so the
 // result carries ~2^-40 of the chunk products' magnitude.  At the end of
-// the tile the totals are converted to FP64, staged in shared memory and
-// written as 64-byte runs of 8 mu per (i, alpha).
+// the tile the totals are converted to FP64 (bits moved, one FP64 add: the
+// FP64 pipe is slow on GB300), staged in shared memory and written as
+// 64-byte runs of 8 mu per (i, alpha).
 // Roles: warps 0-15 converters (row r = 32 (w & 3) + lane, K quarter w >> 2
 // of each chunk: 16 values a thread), warp 16 MMA issuer and TMEM owner.
 // The converter warps are also the epilogue: each is bound to the TMEM lane
 // quadrant of its rows and takes a quarter of the NT columns; in iteration
 // c they slice chunk c and then fold chunk c-1's accumulators into the
-// running totals, while the tensor core runs chunk c.  Each thread copies
-// its 16 values of the next chunk into the FP64 slot (cp.async) once it has
-// handed the current chunk to the tensor core, and every thread prefetches
-// the chunk after that into L2.  Measured (clock64 per role, nbas=680): the
-// converter warps bound the kernel -- slicing and epilogue ~15k cycles per
-// 64-value chunk with four warps per scheduler, latency-bound at ~0.3
-// instructions per cycle -- while the copies wait ~100 cycles a chunk.
-// Every wait is bounded; on expiry
-// the CTA records an error code, drains its copies and MMAs and returns.
+// running totals, while the tensor core runs chunk c.  The four warps of a
+// row group synchronise among themselves only (the chunk maxima exchange),
+// so the groups' latency-bound phases interleave; a group's next box is
+// requested as soon as its warps hold their values (the cp.async form
+// copies after the chunk is handed to the tensor core and prefetches the
+// chunk after that into L2).  The converter warps bound the kernel (issue
+// about 44% active; 3.11 ms at nbas=680, 6.45 ms with all 16 warps in
+// lockstep, a 64-bit integer split, cp.async copies and FP64-pipe
+// conversions).  Every wait is bounded; on expiry the CTA records an error
+// code, drains its copies and MMAs and returns.
 // --------------------------------------------------------------------------
 constexpr int AH_TA = 16, AH_TM = 8;  // alpha x mu rows of a tile (16 x 8 = 128)
 constexpr int AH_CONV = 16;
