@@ -320,7 +320,13 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Philox4x32-10 + Box-Muller, configuration distributions)",
         "config": {"workload": WORKLOAD + "; CPU reference path on a bounded sample of pairs",
-                   "nocc": NOCC, "nvirt": NVIRT, "NBA": NBA, "parallelism": "host OpenMP"},
+                   "nocc": NOCC, "nvirt": NVIRT, "NBA": NBA, "parallelism": "host OpenMP",
+                   # the rate is measured on 2 of the fragment's NOCC^2 ordered
+                   # pairs per step; the whole fragment is this many times the
+                   # sampled work (its time at the same rate)
+                   "sample_pairs_per_step": 2,
+                   "extrapolation_factor": NOCC * NOCC / 2.0,
+                   "extrapolated_full_step_s": ms * 1e-3 * NOCC * NOCC / 2.0},
         "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
                          "sample": desc + "; RIMP2.F90 CPU path restated in C (no Fortran "
                                           "compiler on the box), faithful alpha loop order"},
