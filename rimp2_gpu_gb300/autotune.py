@@ -3,11 +3,15 @@
 Below 16 virtuals, and below 64 (a,i) columns (nocc*nvirt), fragments run
 in FP64 (slice count 0, fixed rules in the library).  For
 each larger virtual-space bucket it runs representative seeded fragments on the
-GPU three ways -- the plain FP64 kernel (the reference values) and the split
-kernel with one and with two residual slices -- and picks the cheapest slice
-count whose worst pair-energy relative error over the sample stays below
-half of the 1e-7 target (a 2x margin for fragments not in the sample).  It
-also records the split kernel's time per bucket.
+GPU four ways -- the plain FP64 kernel (the reference values), the split
+kernel with one residual slice on the kernel the table picks and on the
+one-CTA kernel alone (four products per element pair: more accurate than the
+paired kernel's three), and with two residual slices -- and picks the
+cheapest form whose worst pair-energy relative error over the sample stays
+below half of the 1e-7 target (a 2x margin for fragments not in the
+sample): one slice if either one-slice run qualifies (with the one-CTA
+kernel forced for the bucket if only that run does), else two.  It also
+records the split kernel's time per bucket.
 
 For every bucket that runs one residual slice it then picks the energy
 kernel, i.e. the tile shape: the one-CTA kernel (128 x 128 tiles, four
@@ -70,26 +74,41 @@ def _run(nocc, nvirt, NBA, seed):
         deo = torch.empty(nocc, dtype=torch.float64, device="cuda")
         dev = torch.empty(nvirt, dtype=torch.float64, device="cuda")
         out = {k: (torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda"),
-                   torch.zeros(1, dtype=torch.float64, device="cuda")) for k in (0, 1, 2)}
+                   torch.zeros(1, dtype=torch.float64, device="cuda")) for k in (0, 1, 2, "1o")}
     api.gen_fragment_dev(seed, nocc, nvirt, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(),
                          stream=s)
     E, T = out[0]
     api.energy_dev(nvirt, nocc, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(), E.data_ptr(),
                    T.data_ptr(), precision=api.PREC_FP64, stream=s)
     res = {}
-    for ns in (1, 2):
-        E2, T2 = out[ns]
-        args = (nvirt, nocc, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(), E2.data_ptr(),
-                T2.data_ptr())
-        api.energy_split_dev(*args, nslices=ns, stream=s)  # warm
-        st.synchronize()
-        t0 = time.perf_counter()
-        api.energy_split_dev(*args, nslices=ns, stream=s)
-        st.synchronize()
-        res[ns] = {"ms": (time.perf_counter() - t0) * 1e3}
+    old = os.environ.get("RIMP2_PAIR_KERNEL")
+    try:
+        # one residual slice with the kernel table's choice, one residual slice
+        # on the one-CTA kernel (four products), two residual slices
+        for key, ns in ((1, 1), ("1o", 1), (2, 2)):
+            if key == "1o":
+                os.environ["RIMP2_PAIR_KERNEL"] = "0"
+            E2, T2 = out[key]
+            args = (nvirt, nocc, NBA, dC.data_ptr(), deo.data_ptr(), dev.data_ptr(), E2.data_ptr(),
+                    T2.data_ptr())
+            api.energy_split_dev(*args, nslices=ns, stream=s)  # warm
+            st.synchronize()
+            t0 = time.perf_counter()
+            api.energy_split_dev(*args, nslices=ns, stream=s)
+            st.synchronize()
+            res[key] = {"ms": (time.perf_counter() - t0) * 1e3}
+            if old is None:
+                os.environ.pop("RIMP2_PAIR_KERNEL", None)
+            else:
+                os.environ["RIMP2_PAIR_KERNEL"] = old
+    finally:
+        if old is None:
+            os.environ.pop("RIMP2_PAIR_KERNEL", None)
+        else:
+            os.environ["RIMP2_PAIR_KERNEL"] = old
     api.sync_status(s)
     ref = E.cpu().numpy()
-    for ns in (1, 2):
+    for ns in (1, "1o", 2):
         e = out[ns][0].cpu().numpy()
         res[ns]["pair_max"] = float(np.max(np.abs(e - ref) / np.abs(ref)))
         res[ns]["total"] = abs(out[ns][1].item() - T.item()) / abs(T.item())
@@ -249,17 +268,34 @@ def tune_kernels(buckets, seed=91):
     fitted per bucket to isolated shapes, then that table and uniform
     tables timed on a mixed batch of uneven fragments, whose graph-launched
     persistent groups are what a batch runs; the fastest table is kept."""
-    grid = _grid_rule(buckets, seed)
+    forced = sorted(b["nvirt_min"] for b in buckets if b.get("one_cta_only"))
+    grid = _grid_rule([b for b in buckets if not b.get("one_cta_only")], seed)
     strip = lambda t: [{k: x[k] for k in ("nvirt_min", "min_nocc", "min_nba")} for x in t]  # noqa: E731
-    cands = {"grid_fit": strip(grid), "one_cta_only": [dict(nvirt_min=0, min_nocc=NEVER,
-                                                           min_nba=NEVER)]}
+    edges = sorted({0} | {b["nvirt_min"] for b in buckets})
+
+    def with_forced(table):
+        """The candidate's thresholds at every bucket edge, the one-CTA
+        kernel only in buckets whose one-slice form is accurate enough only
+        with its four products."""
+        out = []
+        for lo in edges:
+            r = max((x for x in table if x["nvirt_min"] <= lo), key=lambda x: x["nvirt_min"])
+            never = lo in forced
+            out.append(dict(nvirt_min=lo, min_nocc=NEVER if never else r["min_nocc"],
+                            min_nba=NEVER if never else r["min_nba"]))
+        return out
+
+    cands = {"grid_fit": with_forced(strip(grid)),
+             "one_cta_only": with_forced([dict(nvirt_min=0, min_nocc=NEVER, min_nba=NEVER)])}
     for mo in (8, 10, 16, 24):
         for mb in (512, 1024, 1536):
-            cands[f"nocc>={mo},NBA>={mb}"] = [dict(nvirt_min=0, min_nocc=mo, min_nba=mb)]
+            cands[f"nocc>={mo},NBA>={mb}"] = with_forced([dict(nvirt_min=0, min_nocc=mo,
+                                                               min_nba=mb)])
     times = _time_mixed_batch(cands)
     best = min(times, key=times.get)
     table = [dict(x, chosen_by=best) for x in cands[best]]
-    return table, {"chosen": best, "mixed_batch": {"fragments": MIX_N, "seed": MIX_SEED,
+    return table, {"chosen": best, "one_cta_only_buckets": forced,
+                   "mixed_batch": {"fragments": MIX_N, "seed": MIX_SEED,
                                                      "shapes": "nocc U[8,64], nvirt U[64,512], "
                                                                "NBA U[256,2048]"},
                    "batch_ms": times, "grid_fit": grid}
@@ -268,17 +304,22 @@ def tune_kernels(buckets, seed=91):
 def tune(seed=77):
     table = []
     for k, lo in enumerate(BUCKET_EDGES):
-        worst = {1: 0.0, 2: 0.0}
-        ms = {1: 0.0, 2: 0.0}
+        worst = {1: 0.0, "1o": 0.0, 2: 0.0}
+        ms = {1: 0.0, "1o": 0.0, 2: 0.0}
         for n, (nocc, nvirt, NBA) in enumerate(SAMPLE[lo]):
             r = _run(nocc, nvirt, NBA, seed + 100 * k + n)
-            for ns in (1, 2):
+            for ns in (1, "1o", 2):
                 worst[ns] = max(worst[ns], r[ns]["pair_max"], r[ns]["total"])
                 ms[ns] += r[ns]["ms"]
-        pick = 1 if worst[1] <= TARGET / 2 else 2
+        # one residual slice (either kernel) performs 3-4 products per
+        # element pair, two slices 6: the first form within the margin wins
+        ok1, ok1o = worst[1] <= TARGET / 2, worst["1o"] <= TARGET / 2
+        pick = 1 if (ok1 or ok1o) else 2
         table.append({"nvirt_min": lo if k else FP64_BELOW, "nslices": pick,
-                      "worst_rel_err": {"1": worst[1], "2": worst[2]},
-                      "split_ms": {"1": ms[1], "2": ms[2]}, "sample": SAMPLE[lo]})
+                      "one_cta_only": bool(pick == 1 and not ok1),
+                      "worst_rel_err": {"1": worst[1], "1_one_cta": worst["1o"], "2": worst[2]},
+                      "split_ms": {"1": ms[1], "1_one_cta": ms["1o"], "2": ms[2]},
+                      "sample": SAMPLE[lo]})
     fixed = {"nvirt_min": 0, "nslices": 0,
              "rule": f"fragments with fewer than {FP64_BELOW} virtuals run in FP64: a pair "
                      "energy of a few g^2 terms has nothing to average the split form's "

@@ -957,9 +957,12 @@ int rimp2_energy_dev(int nvirt, int nocc, int NBA, const double *dCalpha, const 
 // correction term with nothing to average against (1.5e-5 measured at
 // nvirt = 1).  Buckets are keyed by nvirt (the (a,b) count per pair).
 // Default = the table measured by rimp2_gpu_gb300/autotune.py on GB300 with a
-// 2x margin on the 1e-7 target (rimp2_gpu_gb300/tuning/split_buckets.json);
-// rimp2_set_split_buckets replaces it.
-static std::vector<std::pair<int, int>> g_buckets = {{0, 0},   {16, 2},  {128, 2},
+// 2x margin on the 1e-7 target (rimp2_gpu_gb300/tuning/split_buckets.json):
+// the 128-191 bucket takes one slice only on the one-CTA kernel (its four
+// products: 4.2e-8 worst; the paired kernel's three: 6.1e-8), which the
+// kernel table below enforces for that bucket; rimp2_set_split_buckets
+// replaces it.
+static std::vector<std::pair<int, int>> g_buckets = {{0, 0},   {16, 2},  {128, 1},
                                                      {192, 1}, {256, 1}, {384, 1}};
 static std::mutex g_bucket_mu;
 
@@ -1011,7 +1014,9 @@ int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices) {
 struct KernelRule {
   int nvirt_min, min_nocc, min_nba;
 };
-static std::vector<KernelRule> g_krule = {{0, 16, 512}};
+static std::vector<KernelRule> g_krule = {{0, 8, 1024},          {16, 8, 1024},
+                                           {128, 1 << 30, 1 << 30}, {192, 8, 1024},
+                                           {256, 8, 1024},          {384, 8, 1024}};
 
 }  // extern "C"
 
