@@ -1014,9 +1014,9 @@ int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices) {
 struct KernelRule {
   int nvirt_min, min_nocc, min_nba;
 };
-static std::vector<KernelRule> g_krule = {{0, 8, 1024},          {16, 8, 1024},
-                                           {128, 1 << 30, 1 << 30}, {192, 8, 1024},
-                                           {256, 8, 1024},          {384, 8, 1024}};
+static std::vector<KernelRule> g_krule = {{0, 16, 1024},          {16, 16, 1024},
+                                           {128, 1 << 30, 1 << 30}, {192, 16, 1024},
+                                           {256, 16, 1024},         {384, 12, 1024}};
 
 }  // extern "C"
 
