@@ -3540,6 +3540,17 @@ int rcp_denom_selftest(int n, const float *d, float *r, float *ref, cudaStream_t
 // while chunk c+1 is still in flight.  dCa must have room for the fragment.
 int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs &a,
                           cudaStream_t s, cudaStream_t copy_s, int chunk_occ) {
+  // Occupied-index chunk boundaries: the first chunk small (its copy is the
+  // only one nothing hides), later ones growing by half, since chunk c's
+  // work grows with its column indices j while its copy does not; chunk_occ
+  // caps the first chunk.  The energy of chunk c starts as soon as its copy
+  // lands, so after the first few chunks the copy engine runs ahead.
+  std::vector<int> bnd;
+  for (int b = std::min(a.nocc, std::max(1, std::min(chunk_occ, 4))); ;) {
+    bnd.push_back(b);
+    if (b >= a.nocc) break;
+    b = std::min(a.nocc, b + std::max(1, b / 2));
+  }
   if (inject_fault("launch")) {  // before any copy is in flight
     set_error("injected launch failure (RIMP2_FAULT_INJECT=launch)");
     return RIMP2_ERR_CUDA;
@@ -3553,7 +3564,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   const FragDesc &F = g.fh[0];
   const FragDesc *fr = g.frags.as<FragDesc>();
   int rc = RIMP2_OK;
-  const int nchunk = (a.nocc + chunk_occ - 1) / chunk_occ;
+  const int nchunk = (int)bnd.size();
   std::vector<cudaEvent_t> ev(nchunk, nullptr);
   for (auto &e : ev)
     if (rc == RIMP2_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
@@ -3563,7 +3574,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   const size_t slab = (size_t)a.NBA * a.nvirt;  // doubles per occupied index
   // copies first, so the copy engine runs ahead of the compute stream
   for (int c = 0; c < nchunk && rc == RIMP2_OK; ++c) {
-    const int i0 = c * chunk_occ, i1 = std::min(a.nocc, i0 + chunk_occ);
+    const int i0 = c ? bnd[c - 1] : 0, i1 = bnd[c];
     cudaError_t e = cudaMemcpyAsync(dCa + slab * i0, hCa + slab * i0, sizeof(double) * slab * (i1 - i0),
                                     cudaMemcpyHostToDevice, copy_s);
     if (e == cudaSuccess) e = cudaEventRecord(ev[c], copy_s);
@@ -3586,7 +3597,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   BP.part = g.part.as<double>();
   BP.err = device_error_word();
   for (int c = 0; c < nchunk && rc == RIMP2_OK; ++c) {
-    const int i0 = c * chunk_occ, i1 = std::min(a.nocc, i0 + chunk_occ);
+    const int i0 = c ? bnd[c - 1] : 0, i1 = bnd[c];
     cudaError_t e = cudaStreamWaitEvent(s, ev[c], 0);
     if (e != cudaSuccess) {
       set_error("stream wait failed: %s", cudaGetErrorString(e));
