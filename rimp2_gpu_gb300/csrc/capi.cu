@@ -1009,8 +1009,9 @@ int rimp2_set_split_buckets(int n, const int *nvirt_min, const int *nslices) {
 // spaces and few occupied orbitals.  Default = the table chosen by
 // rimp2_gpu_gb300/autotune.py on GB300 (rimp2_gpu_gb300/tuning/
 // split_buckets.json, "kernel_rule": fitted per bucket on isolated shapes,
-// then selected among candidate tables on a mixed batch, where one uniform
-// table matched the per-bucket fit); rimp2_set_split_kernel_rule replaces it.
+// then selected among candidate tables on a mixed batch of uneven
+// fragments, with the 128-191 bucket held on the one-CTA kernel for its
+// accuracy); rimp2_set_split_kernel_rule replaces it.
 struct KernelRule {
   int nvirt_min, min_nocc, min_nba;
 };
