@@ -2386,8 +2386,9 @@ int record_group(Group &g, cudaStream_t s, int nsm, cudaEvent_t *ev /* 3 or null
 // tiles.  Per K16 step one MMA over the stacked B planes [S0b; R1b] (N = 2 NT)
 // gives L0 and S0a R1b, then R1a S0b, R1a R1b (and S0a R2b, R2a S0b with two
 // residual slices) accumulate into L1.
-// Roles: warp 0 TMA producer, warp 1 MMA issuer and TMEM owner, warps 2-5
-// epilogue (one per TMEM lane quadrant).  Every wait is bounded.
+// Roles: warp 0 TMA producer, warp 1 MMA issuer and TMEM owner, warps 2-9
+// epilogue (two per TMEM lane quadrant, alternate 16-column chunks).  Every
+// wait is bounded.
 // ==========================================================================
 struct GemmSP {
   int M, N, NT, nks, mtiles, ntiles, nbatch;
@@ -2408,8 +2409,11 @@ constexpr int gemm_smem_bytes(int nsl, int NT) {
   return GEMM_NST * gemm_stage_bytes(nsl, NT) + 1024 + 256;
 }
 
+constexpr int GEMM_EPI = 8;                       // epilogue warps: two per lane quadrant
+constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI;
+
 template <int NSL>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       GemmSP P) {
   constexpr int NST = GEMM_NST;
@@ -2435,7 +2439,7 @@ __global__ void __launch_bounds__(192, 1)
     }
     for (int u = 0; u < 2; ++u) {
       mbar_init(tfull0 + 8 * u, 1);
-      mbar_init(tempty0 + 8 * u, 4);  // the four epilogue warps
+      mbar_init(tempty0 + 8 * u, GEMM_EPI);  // the epilogue warps
     }
     mbar_init(drain, 1);
     *abort_flag = 0;
@@ -2563,6 +2567,7 @@ __global__ void __launch_bounds__(192, 1)
   } else {
     // ------------------------------ epilogue ----------------------------------
     const int quad = warp & 3;
+    const int half = (warp - 2) >> 2;  // 16-column chunks half, half + 2, ...
     const int row = quad * 32 + lane;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     long long t = 0;
@@ -2577,7 +2582,7 @@ __global__ void __launch_bounds__(192, 1)
       const float sa = P.a_inv[arow + row];  // 2^-e of this row
       const uint32_t taddr = tmem + lane_off + (uint32_t)(u * 2 * NT);
       double *orow = P.out + (long long)b * P.sOb + m * P.sOm;
-      for (int c0 = 0; c0 < NT; c0 += 16) {
+      for (int c0 = 16 * half; c0 < NT; c0 += 32) {
         float l0[16], l1[16];
         tmem_ld16(taddr + c0, l0);
         tmem_ld16(taddr + NT + c0, l1);
@@ -3803,11 +3808,11 @@ int split_gemm(const SlicedOp &A, long long a_row0, long long a_bstride, const S
   int dev = 0, nsm = 0, resident = 0;
   RIMP2_CK(cudaGetDevice(&dev));
   RIMP2_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 192, smem));
+  RIMP2_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, GEMM_THREADS, smem));
   // persistent CTAs whose TMEM allocations fit an SM together
   resident = std::max(1, std::min(resident, (int)(512 / cols)));
   const long long grid = std::min<long long>(nitems, (long long)nsm * resident);
-  kern<<<(unsigned)grid, 192, smem, s>>>(tA, tB, P);
+  kern<<<(unsigned)grid, GEMM_THREADS, smem, s>>>(tA, tB, P);
   count_launch(1);
   RIMP2_CK(cudaGetLastError());
   return RIMP2_OK;
