@@ -404,20 +404,28 @@ __device__ __forceinline__ void split_int(unsigned long long b, int e, float &q,
 
 // Power-of-two scale exponent of a column from its largest magnitude (bits)
 // and its FP32 sum of squares: |C 2^e| <= 2047.5 and ||C 2^e||_2 below 2^12
-// with room for the rounding of NBA values.  FP64 arithmetic, which GB300
-// runs at a small fraction of its FP32 rate: one thread per column calls it.
+// with room for the rounding of NBA values.  Integer and FP32 arithmetic only
+// (GB300's FP64 pipe is a small fraction of its FP32 rate, and the FP64
+// sqrt/div/log2 of this choice, once per column, bounded the slicing
+// kernels): with max |C| = m 2^E (m in [1, 2)), 2047.5 / m lies in
+// (1023.75, 2047.5], so the magnitude bound allows e = 10 - E when m <=
+// 2047.5 / 1024 = 2 - 2^-11 (fraction bits <= 0xFFE00 << 32) and 9 - E
+// otherwise; the norm bound takes the binary exponent of the FP32 ratio,
+// correctly rounded operations with a 2^-20 margin (float
+// truncation of the squares underestimates ||C||^2 by < 2^-21 relative; the
+// caller's exact integer check of ||S0||^2 keeps the exactness either way).
+// Clamped to [-100, 100]; 0 for an all-zero column.
 __device__ __forceinline__ int col_scale_exponent(unsigned long long mxb, float ss, int NBA) {
-  const double mx = __longlong_as_double((long long)mxb);
-  int e = 0;
-  if (mx > 0.0) {
-    // float truncation of the squares underestimates ||C||^2 by < 2^-21
-    // relative; the exact integer check of the caller keeps the exactness
-    const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
-    const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)NBA)) / nrm);
-    e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
-    e = max(-100, min(100, e));
+  if (mxb == 0) return 0;
+  const int ed = (int)(mxb >> 52);
+  if (ed == 0) return 100;  // largest value subnormal
+  const int e1 = ((mxb & 0xFFFFFFFFFFFFFull) <= (0xFFE00ull << 32) ? 10 : 9) - (ed - 1023);
+  int e2 = 127;
+  if (ss > 0.0f) {
+    const float r = (4096.0f - 0.5f * sqrtf((float)NBA)) / sqrtf(ss) * 0.99999905f;
+    e2 = (int)((__float_as_uint(r) >> 23) & 0xFFu) - 127;  // floor(log2 r) for r normal
   }
-  return e;
+  return max(-100, min(100, min(e1, e2)));
 }
 
 // Slices of every fragment: slice plane s, fragment f, K chunk kc, column c
@@ -3236,13 +3244,7 @@ __global__ void __launch_bounds__(AO_ROWS) ao_slice_kernel(const double *__restr
         ss = fmaf(f, f, ss);
       }
     }
-    const double mx = __longlong_as_double((long long)mxb);
-    if (mx > 0.0) {
-      const double nrm = sqrt((double)ss) * (1.0 + 1e-6) + 1e-300;
-      const double lim = fmin(2047.5 / mx, (4096.0 - 0.5 * sqrt((double)nbas)) / nrm);
-      e = (lim > 0.0 && lim < 1e300) ? (int)floor(log2(lim)) : -100;
-      e = max(-100, min(100, e));
-    }
+    e = col_scale_exponent(mxb, ss, nbas);
   }
   const int rl = m_l + AO_TM * a_l;  // row within the CTA: the 8 mu of one alpha adjacent
   const int sw = a_l & 7;

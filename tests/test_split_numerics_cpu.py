@@ -115,3 +115,53 @@ def test_fp32_split_of_doubles_against_exact_arithmetic():
             assert err <= Fraction(abs(float(r))) * Fraction(1, 2 ** 24) + Fraction(1, 2 ** 36)
             if abs(v) >= 1:
                 assert abs(Fraction(float(r))) <= Fraction(1, 2) + Fraction(1, 2 ** 20)
+
+
+def col_scale_exponent_emulated(mx, ss, K):
+    """The slicers' column exponent in integer and FP32 arithmetic (numpy
+    float32 operations are correctly rounded, like the kernel's sqrtf and
+    division)."""
+    if mx == 0.0:
+        return 0
+    b = int(np.float64(mx).view(np.uint64))
+    ed = b >> 52
+    if ed == 0:
+        return 100
+    e1 = (10 if (b & ((1 << 52) - 1)) <= (0xFFE00 << 32) else 9) - (ed - 1023)
+    e2 = 127
+    ss = np.float32(ss)
+    if ss > 0:
+        f = np.float32
+        r = (f(4096.0) - f(0.5) * np.sqrt(f(K))) / np.sqrt(ss) * f(0.99999905)
+        e2 = int((int(np.float32(r).view(np.uint32)) >> 23) & 0xFF) - 127
+    return max(-100, min(100, min(e1, e2)))
+
+
+def test_column_exponent_without_fp64_math():
+    """The integer/FP32 exponent keeps |C 2^e| <= 2047.5 exactly and the
+    column norm within 4096 - sqrt(K)/2, and is the FP64 formula's exponent
+    or one below it (the FP32 margin)."""
+    rng = np.random.default_rng(11)
+    lower = 0
+    for t in range(3000):
+        K = int(rng.integers(1, 5000))
+        scale = 10.0 ** rng.uniform(-15, 15)  # squares within FP32 range
+        C = rng.standard_normal(K) * scale
+        if t % 3 == 0:  # a dominant element with mantissa near 2 - 2^-11
+            m = float(rng.choice([2 - 2.0 ** -11, np.nextafter(2 - 2.0 ** -11, 2), 1.0, 1.9995]))
+            C[int(rng.integers(K))] = np.ldexp(m, int(np.floor(np.log2(scale))) + 4)
+        mx = float(np.abs(C).max())
+        ss = float(np.float32((C * C).sum()))
+        nrm = np.sqrt(ss) * (1.0 + 1e-6)
+        lim = min(2047.5 / mx, (4096.0 - 0.5 * np.sqrt(K)) / nrm)
+        e_old = max(-100, min(100, int(np.floor(np.log2(lim)))))
+        e = col_scale_exponent_emulated(mx, ss, K)
+        assert mx * 2.0 ** e <= 2047.5
+        assert np.sqrt((C * C).sum()) * 2.0 ** e <= 4096.0 - 0.5 * np.sqrt(K)
+        assert e_old - 1 <= e <= e_old
+        # the FP64 formula's 2047.5 / mx rounds up to a power of two for a
+        # mantissa just above 2 - 2^-11, where its exponent breaks the bound
+        lower += e < e_old and mx * 2.0 ** e_old <= 2047.5
+    assert lower < 10  # the FP32 margin costs a bit only near a power of two
+    assert col_scale_exponent_emulated(0.0, 0.0, 64) == 0
+    assert col_scale_exponent_emulated(np.float64(1e-310), 0.0, 64) == 100
