@@ -907,6 +907,26 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
             fe_ms.append(fe)
             en_ms.append(e0.elapsed_time(e1))
     launches = api.kernel_launch_count() - n0
+    # the transform alone (no Cholesky beside it), on the last fragment's AO
+    # tensor, still in place; the tensor exceeds L2, so every run reads HBM
+    nbas_l, nba_l, nocc_l, nvirt_l = shapes[-1]
+    alone = []
+    for _ in range(3):
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        api.ao2mo_dev(nba_l, nbas_l, nocc_l, nvirt_l, ao.data_ptr(), frags[-1]["Cmo"].data_ptr(),
+                      Bw.data_ptr(), split=(transform == "split"), stream=sp)
+        a1.record(st)
+        st.synchronize()
+        alone.append(a0.elapsed_time(a1))
+    alone_ms = statistics.median(alone[1:])
+    alone_bytes = 8.0 * nba_l * nbas_l * nbas_l + 8.0 * nba_l * nvirt_l * nocc_l
+    hbm = None
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as f:
+            hbm = json.load(f).get("hbm_gbs")
     fe_m, en_m = statistics.median(fe_ms), statistics.median(en_ms)
     tr_m = statistics.median(p[0] for p in parts_ms)
     ch_m = statistics.median(p[1] for p in parts_ms)
@@ -942,6 +962,13 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
             "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
             "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
             "transform_algorithmic_bytes": ao_bytes,
+            "transform_alone": {
+                "ms": alone_ms, "shape_nbas_nba_nocc_nvirt": [nbas_l, nba_l, nocc_l, nvirt_l],
+                "algorithmic_gbs": alone_bytes / (alone_ms * 1e-3) / 1e9,
+                "frac_of_measured_hbm": (alone_bytes / (alone_ms * 1e-3) / 1e9 / hbm
+                                         if hbm else None),
+                "note": "one fragment's transform with nothing beside it (median of the last "
+                        "two of three runs; the AO tensor exceeds L2)"},
             "cholesky_fp64_tflops": ch_flop / (ch_m * 1e-3) / 1e12,
             "solve_fp64_tflops": so_flop / (so_m * 1e-3) / 1e12,
             "solve_performed_fp64_tflops": so_perf / (so_m * 1e-3) / 1e12,
