@@ -259,7 +259,13 @@ int rimp2_energy_split_dev(int nvirt, int nocc, int NBA, const double *dCalpha,
 /* Many DEC fragments of uneven size in one call.  Fragment f has sizes
  * nocc[f], nvirt[f], NBA[f]; its Calpha/EVocc/EVvirt start at the given
  * element offsets into the concatenated host arrays; Epair of fragment f
- * starts at epair_off[f] (nocc[f]^2 entries), Etot[f] is its total. */
+ * starts at epair_off[f] (nocc[f]^2 entries), Etot[f] is its total.  The
+ * fragments are copied to the device launch group by launch group (the
+ * group with the least Calpha first) on the library's copy stream, and each
+ * group's kernels wait only for its own fragments: with Calpha in pinned
+ * host memory the copies are asynchronous and the transfer of later groups
+ * overlaps the kernels of earlier ones (pageable memory is copied through
+ * the driver's staging, before the kernels start). */
 int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, const int *NBA,
                          const double *Calpha, const long long *calpha_off, const double *EVocc,
                          const long long *eo_off, const double *EVvirt, const long long *ev_off,

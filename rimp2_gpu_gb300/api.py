@@ -250,18 +250,37 @@ def energy_split_dev(nvirt, nocc, NBA, dCalpha, dEVocc, dEVvirt, dEpair, dEtot, 
 
 def energy_batched(frags, precision=PREC_FP64):
     """frags: list of (Calpha, EVocc, EVvirt) numpy arrays of uneven sizes.
-    Returns a list of (Epair, Etot)."""
-    nf = len(frags)
-    nocc = np.array([f[1].size for f in frags], dtype=np.int32)
-    nvirt = np.array([f[2].size for f in frags], dtype=np.int32)
-    nba = np.array([f[0].shape[0] for f in frags], dtype=np.int32)
+    Returns a list of (Epair, Etot).  The fragments are packed into one
+    array first (a host copy); energy_batched_packed takes packed input."""
+    nocc = [f[1].size for f in frags]
+    nvirt = [f[2].size for f in frags]
+    nba = [f[0].shape[0] for f in frags]
     ca = np.concatenate([np.asfortranarray(f[0]).ravel(order="F") for f in frags])
     eo = np.concatenate([f[1] for f in frags])
     ev = np.concatenate([f[2] for f in frags])
-    off = lambda sizes: np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)  # noqa: E731
-    ca_off = off([f[0].size for f in frags])
-    eo_off = off(nocc)
-    ev_off = off(nvirt)
+    return energy_batched_packed(nocc, nvirt, nba, ca, eo, ev, precision)
+
+
+def energy_batched_packed(nocc, nvirt, nba, ca, eo, ev, precision=PREC_FP64):
+    """Batched energies of fragments packed back to back in host memory:
+    ``ca`` holds each fragment's Calpha(NBA, nvirt, nocc) (column-major) in
+    turn, ``eo``/``ev`` their occupied/virtual orbital energies.  The library
+    copies fragment by fragment, launch group by launch group, and each
+    group's kernels wait only for its own copies: with ``ca`` in pinned
+    memory (e.g. a ``torch.empty(..., pin_memory=True)`` tensor's numpy
+    view) the transfer of later groups overlaps the kernels of earlier ones.
+    Returns a list of (Epair, Etot)."""
+    nocc = np.ascontiguousarray(nocc, dtype=np.int32)
+    nvirt = np.ascontiguousarray(nvirt, dtype=np.int32)
+    nba = np.ascontiguousarray(nba, dtype=np.int32)
+    nf = len(nocc)
+    if not (len(nvirt) == len(nba) == nf):
+        raise ValueError("nocc, nvirt and nba must have one entry per fragment")
+    sizes = nba.astype(np.int64) * nvirt * nocc
+    off = lambda v: np.concatenate([[0], np.cumsum(v)[:-1]]).astype(np.int64)  # noqa: E731
+    if ca.size != int(sizes.sum()) or eo.size != int(nocc.sum()) or ev.size != int(nvirt.sum()):
+        raise ValueError("packed Calpha / orbital energies do not match the fragment sizes")
+    ca_off, eo_off, ev_off = off(sizes), off(nocc), off(nvirt)
     ep_off = off(nocc.astype(np.int64) ** 2)
     Ep = np.zeros(int((nocc.astype(np.int64) ** 2).sum()), dtype=np.float64)
     Et = np.zeros(nf, dtype=np.float64)

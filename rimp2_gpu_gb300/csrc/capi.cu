@@ -1223,7 +1223,11 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
   RIMP2_TRY(ensure_device());
   cudaStream_t s = current_stream();
   // one device copy of every fragment (inputs are in HBM together; the
-  // split form then runs the batch as one persistent launch per kernel group)
+  // split form then runs the batch as one persistent launch per kernel
+  // group).  The plan is built on the destination addresses first; the
+  // copies then run on the copy stream group by group, each group's kernels
+  // waiting only for its own fragments (host memory pinned by the caller
+  // makes the copies asynchronous, so they overlap the earlier groups)
   size_t nca = 0, neo = 0, nev = 0, nep = 0;
   for (int f = 0; f < nf; ++f) {
     nca += (size_t)NBA[f] * nvirt[f] * nocc[f];
@@ -1239,15 +1243,20 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
   RIMP2_TRY(dalloc(dT, nf, s));
   std::vector<const double *> pc(nf), peo(nf), pev(nf);
   std::vector<double *> pE(nf), pT(nf);
+  std::vector<double *> cdst;
+  std::vector<const double *> csrc;
+  std::vector<size_t> ccount;
+  auto copy = [&](double *d, const double *h, size_t n) {
+    cdst.push_back(d);
+    csrc.push_back(h);
+    ccount.push_back(n);
+  };
   size_t oc = 0, oo = 0, ov = 0, oe = 0;
   for (int f = 0; f < nf; ++f) {
     const size_t n = (size_t)NBA[f] * nvirt[f] * nocc[f];
-    RIMP2_CK(cudaMemcpyAsync(dC.as<double>() + oc, Calpha + calpha_off[f], n * 8,
-                             cudaMemcpyHostToDevice, s));
-    RIMP2_CK(cudaMemcpyAsync(deo.as<double>() + oo, EVocc + eo_off[f], (size_t)nocc[f] * 8,
-                             cudaMemcpyHostToDevice, s));
-    RIMP2_CK(cudaMemcpyAsync(dev.as<double>() + ov, EVvirt + ev_off[f], (size_t)nvirt[f] * 8,
-                             cudaMemcpyHostToDevice, s));
+    copy(dC.as<double>() + oc, Calpha + calpha_off[f], n);
+    copy(deo.as<double>() + oo, EVocc + eo_off[f], (size_t)nocc[f]);
+    copy(dev.as<double>() + ov, EVvirt + ev_off[f], (size_t)nvirt[f]);
     pc[f] = dC.as<double>() + oc;
     peo[f] = deo.as<double>() + oo;
     pev[f] = dev.as<double>() + ov;
@@ -1267,7 +1276,10 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
                                       pev.data(), pE.data(), pT.data(),
                                       *precision == RIMP2_PREC_SPLIT ? nullptr : zeros.data(), 0,
                                       s));
-    int rc = rimp2_batch_plan_execute(plan, s);
+    cudaStream_t cs = copy_stream();
+    int rc = cs ? split_plan_execute_host((SplitPlan *)plan, s, cs, (int)cdst.size(), cdst.data(),
+                                          csrc.data(), ccount.data())
+                : (set_error("copy stream creation failed"), RIMP2_ERR_CUDA);
     split_plan_destroy((SplitPlan *)plan);  // keeps the error message of a failed execute
     RIMP2_TRY(rc);
   }

@@ -3516,6 +3516,61 @@ int split_plan_execute(SplitPlan *P, cudaStream_t s) {
 
 void split_plan_destroy(SplitPlan *P) { delete P; }
 
+// Execution of a plan (no graph) whose inputs are still in host memory:
+// copy c moves count[c] doubles from src[c] to dst[c].  The copies run on the
+// copy stream cs launch group by launch group, the group with the least
+// Calpha first; copies that belong to no split group (orbital energies, the
+// plain FP64 fragments) go before all of them.  Each group's slicing waits
+// only for its own fragments' copies, so the transfer of the later, larger
+// groups overlaps the kernels of the earlier ones.  A copy belongs to the
+// group whose fragment has dst as its Calpha address.
+int split_plan_execute_host(SplitPlan *P, cudaStream_t s, cudaStream_t cs, int ncopy,
+                            double *const *dst, const double *const *src, const size_t *count) {
+  struct Events {
+    cudaEvent_t e[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    ~Events() {
+      for (auto &x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } ev;
+  for (auto &x : ev.e) RIMP2_CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+  std::vector<int> owner(ncopy, -1);  // launch group of each copy, -1: none
+  size_t bytes[3] = {0, 0, 0};
+  int order[3], n = 0;
+  for (int k = 0; k < 3; ++k) {
+    for (const auto &F : P->g[k].fh) {
+      bytes[k] += (size_t)F.NBA * F.nvirt * F.nocc;
+      for (int c = 0; c < ncopy; ++c)
+        if (dst[c] == F.Ca) owner[c] = k;
+    }
+    if (P->g[k].nfrag) order[n++] = k;
+  }
+  std::sort(order, order + n, [&](int a, int b) { return bytes[a] < bytes[b]; });
+  // the copy stream starts after the destination buffers' allocation on s
+  RIMP2_CK(cudaEventRecord(ev.e[0], s));
+  RIMP2_CK(cudaStreamWaitEvent(cs, ev.e[0], 0));
+  for (int c = 0; c < ncopy; ++c)
+    if (owner[c] < 0)
+      RIMP2_CK(cudaMemcpyAsync(dst[c], src[c], count[c] * sizeof(double), cudaMemcpyHostToDevice,
+                               cs));
+  RIMP2_CK(cudaEventRecord(ev.e[1], cs));
+  for (int k = 0; k < n; ++k) {
+    for (int c = 0; c < ncopy; ++c)
+      if (owner[c] == order[k])
+        RIMP2_CK(cudaMemcpyAsync(dst[c], src[c], count[c] * sizeof(double),
+                                 cudaMemcpyHostToDevice, cs));
+    RIMP2_CK(cudaEventRecord(ev.e[2 + k], cs));
+  }
+  RIMP2_CK(cudaStreamWaitEvent(s, ev.e[1], 0));
+  RIMP2_TRY(plain_plan_record(P->plain, s));
+  for (int k = 0; k < n; ++k) {
+    RIMP2_CK(cudaStreamWaitEvent(s, ev.e[2 + k], 0));
+    RIMP2_TRY(record_group(P->g[order[k]], s, P->nsm, nullptr));
+  }
+  return RIMP2_OK;
+}
+
+
 int bounded_wait_selftest(long long budget_cycles, cudaStream_t s) {
   wait_selftest_kernel<<<1, 32, 0, s>>>(budget_cycles, device_error_word());
   count_launch(1);

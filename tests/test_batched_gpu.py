@@ -132,3 +132,41 @@ def _all_four_groups(api, torch):
         Ep = t["E"].cpu().numpy().reshape(n, n, order="F")
         assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= tol
         assert abs(t["T"].item() - Er) <= tol * abs(Er)
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-11), (1, 1e-7)])
+def test_energy_batched_packed_pinned(prec, tol):
+    """Packed host input in pinned memory through rimp2_energy_batched's
+    overlapped copies (per launch group on the copy stream, each group's
+    kernels waiting for its own fragments).  Split form: every launch group
+    present -- paired kernel (the kernel table set to nocc >= 10, NBA >= 1024
+    here), one-CTA kernel with one and with two residual slices, and plain
+    FP64 (nocc * nvirt < 64); FP64 form: all in the plain launch."""
+    import os
+    import torch
+    from rimp2_gpu_gb300 import api, autotune
+    shapes = [(12, 256, 1024), (11, 200, 300), (5, 130, 777), (8, 64, 256), (2, 20, 100)]
+    data = [O.gen_fragment(900 + k, *s) for k, s in enumerate(shapes)]
+    ref = [O.pair_energies(v, n, b, Ca, eo, ev, blocked=True)
+           for (n, v, b), (Ca, eo, ev) in zip(shapes, data)]
+    ca = torch.empty(sum(n * v * b for n, v, b in shapes), dtype=torch.float64, pin_memory=True)
+    cav, o = ca.numpy(), 0
+    for Ca, _, _ in data:
+        cav[o:o + Ca.size] = Ca.ravel(order="F")
+        o += Ca.size
+    eo = np.concatenate([d[1] for d in data])
+    ev = np.concatenate([d[2] for d in data])
+    api.set_split_kernel_rule([0], [10], [1024])
+    try:
+        assert [api.split_nslices(v, n, b) for n, v, b in shapes] == [1, 1, 1, 2, 0]
+        res = api.energy_batched_packed([s[0] for s in shapes], [s[1] for s in shapes],
+                                        [s[2] for s in shapes], cav, eo, ev, precision=prec)
+    finally:
+        autotune.load(os.path.join(os.path.dirname(api.__file__), "tuning", "split_buckets.json"))
+    for (n, v, b), (Ep, E), (Epr, Er) in zip(shapes, res, ref):
+        bar = 1e-11 if prec == 0 or api.split_nslices(v, n, b) == 0 else tol
+        assert (np.abs(Ep - Epr) / np.abs(Epr)).max() <= bar
+        assert abs(E - Er) <= bar * abs(Er)
+    with pytest.raises(ValueError):
+        api.energy_batched_packed([s[0] for s in shapes], [s[1] for s in shapes],
+                                  [s[2] for s in shapes], cav[:-1], eo, ev, precision=prec)
