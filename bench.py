@@ -84,6 +84,8 @@ def parse():
                     help="batched workload: the first N of the 256 seeded shapes (profiling)")
     ap.add_argument("--ao-fragments", type=int, default=AO_N_DEFAULT,
                     help="fragments in the AO pipeline workload")
+    ap.add_argument("--ao-serial", action="store_true",
+                    help="AO pipeline: run the metric Cholesky after the transform, not beside it")
     ap.add_argument("--ao-transform", choices=["split", "fp64"], default="split",
                     help="AO->MO transform on the tensor cores (split) or in FP64; the metric "
                          "Cholesky and the triangular solve are FP64 either way")
@@ -828,7 +830,7 @@ def mo_coefficients(nbas, seed):
     return np.asfortranarray(q * np.sign(np.diag(r)))
 
 
-def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
+def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None, serial=False):
     """Config 5: per fragment the AO tensor is generated on the device (untimed
     input creation), then Calpha is formed on the GPU (AO->MO transform,
     metric Cholesky, triangular solve; timed), and finally all fragments'
@@ -881,7 +883,7 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
         if step == warmup:
             n0 = api.kernel_launch_count()
         fe = 0.0
-        tr = ch = so = 0.0
+        tr = ch = so = win = 0.0
         for f, (nbas, nba, nocc, nvirt) in enumerate(shapes):
             api.gen_ao_dev(4000 + f, nba, nbas, ao.data_ptr(), V.data_ptr(), stream=sp)
             st.synchronize()  # inputs complete before the timed section
@@ -893,7 +895,7 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
             api.ao2mo_dev(nba, nbas, nocc, nvirt, ao.data_ptr(), frags[f]["Cmo"].data_ptr(),
                           Bw.data_ptr(), split=(transform == "split"), stream=sp)
             ev[1].record(st)
-            st2.wait_event(ev[0])
+            st2.wait_event(ev[1] if serial else ev[0])  # serial: the Cholesky after the transform
             api.cholesky_dev(nba, V.data_ptr(), stream=st2.cuda_stream)
             ev[3].record(st2)
             st.wait_stream(st2)
@@ -905,9 +907,10 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
             tr += ev[0].elapsed_time(ev[1])
             ch += ev[0].elapsed_time(ev[3])
             so += ev[4].elapsed_time(ev[5])
+            win += ev[0].elapsed_time(ev[4])
             fe += ev[0].elapsed_time(ev[5])
         if step >= warmup:
-            parts_ms.append((tr, ch, so))
+            parts_ms.append((tr, ch, so, win))
         if plan is None:
             plan = api.BatchPlan(desc, graph=True, stream=sp)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -935,6 +938,16 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
         st.synchronize()
         alone.append(a0.elapsed_time(a1))
     alone_ms = statistics.median(alone[1:])
+    # the Cholesky alone, on the last fragment's metric generated afresh
+    api.gen_ao_dev(4000 + len(shapes) - 1, nba_l, nbas_l, 0, V.data_ptr(), stream=sp)
+    st.synchronize()
+    c0 = torch.cuda.Event(enable_timing=True)
+    c1 = torch.cuda.Event(enable_timing=True)
+    c0.record(st)
+    api.cholesky_dev(nba_l, V.data_ptr(), stream=sp)
+    c1.record(st)
+    st.synchronize()
+    chol_alone_ms = c0.elapsed_time(c1)
     alone_bytes = 8.0 * nba_l * nbas_l * nbas_l + 8.0 * nba_l * nvirt_l * nocc_l
     hbm = None
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -945,6 +958,7 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
     tr_m = statistics.median(p[0] for p in parts_ms)
     ch_m = statistics.median(p[1] for p in parts_ms)
     so_m = statistics.median(p[2] for p in parts_ms)
+    win_m = statistics.median(p[3] for p in parts_ms)
     ms = allmax(pg, fe_m + en_m)
     acc = None
     if check in ("full", "sample"):
@@ -970,8 +984,9 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
     return {"value": eff / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms,
             "fragments": len(shapes), "shapes_nbas_nba_nocc_nvirt": [list(x) for x in shapes[:4]],
             "ao_transform": transform, "front_end_ms": fe_m, "energy_ms": en_m,
-            "front_end_overlap": "AO->MO transform and metric Cholesky run concurrently "
-                                 "(two streams); parts overlap",
+            "front_end_overlap": ("metric Cholesky after the AO->MO transform" if serial else
+                                  "AO->MO transform and metric Cholesky run concurrently "
+                                  "(two streams); parts overlap"),
             "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,
             "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
             "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
@@ -983,6 +998,9 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
                                          if hbm else None),
                 "note": "one fragment's transform with nothing beside it (median of the last "
                         "two of three runs; the AO tensor exceeds L2)"},
+            "cholesky_alone": {"ms": chol_alone_ms, "fp64_tflops": nba_l ** 3 / 3.0 / chol_alone_ms / 1e9,
+                               "shape_nba": nba_l},
+            "transform_and_cholesky_window_ms": win_m,
             "cholesky_fp64_tflops": ch_flop / (ch_m * 1e-3) / 1e12,
             "solve_fp64_tflops": so_flop / (so_m * 1e-3) / 1e12,
             "solve_performed_fp64_tflops": so_perf / (so_m * 1e-3) / 1e12,
@@ -1002,7 +1020,7 @@ def run_ao(args):
         b = args.ao_nbas
         shapes = [(b, 3 * b, b // 10, b - b // 10)] * len(shapes)
     r = ao_leg(api, torch, dev, shapes, args.steps, args.warmup, args.ao_transform, args.check,
-               pg=pg)
+               pg=pg, serial=args.ao_serial)
     if rank == 0:
         cfg = {k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step",
                                                        "accuracy", "gpu_launches")}
