@@ -146,8 +146,9 @@ int split_plan_create(SplitPlan **out, int nfrag, const int *nocc, const int *nv
                       double *const *Epair, double *const *Etot, const int *nslices, bool graph,
                       cudaStream_t s);
 int split_plan_execute(SplitPlan *P, cudaStream_t s);
-int split_plan_execute_host(SplitPlan *P, cudaStream_t s, cudaStream_t cs, int ncopy,
-                            double *const *dst, const double *const *src, const size_t *count);
+int split_plan_execute_host(SplitPlan *P, cudaStream_t s, const cudaStream_t *cs, int ncs,
+                            int ncopy, double *const *dst, const double *const *src,
+                            const size_t *count, bool wait_alloc = true);
 void split_plan_destroy(SplitPlan *P);
 int bounded_wait_selftest(long long budget_cycles, cudaStream_t s);
 int rcp_denom_selftest(int n, const float *d, float *r, float *ref, cudaStream_t s);

@@ -3518,22 +3518,30 @@ void split_plan_destroy(SplitPlan *P) { delete P; }
 
 // Execution of a plan (no graph) whose inputs are still in host memory:
 // copy c moves count[c] doubles from src[c] to dst[c].  The copies run on the
-// copy stream cs launch group by launch group, the group with the least
-// Calpha first; copies that belong to no split group (orbital energies, the
-// plain FP64 fragments) go before all of them.  Each group's slicing waits
-// only for its own fragments' copies, so the transfer of the later, larger
+// copy streams cs[0..ncs) launch group by launch group, the group with the
+// least Calpha first; copies that belong to no split group (orbital
+// energies, the plain FP64 fragments) go before all of them.  Within a
+// group each copy goes to the stream with the fewest bytes so far, so that
+// several copy engines share the transfer.  Each group's slicing waits only
+// for its own fragments' copies, so the transfer of the later, larger
 // groups overlaps the kernels of the earlier ones.  A copy belongs to the
-// group whose fragment has dst as its Calpha address.
-int split_plan_execute_host(SplitPlan *P, cudaStream_t s, cudaStream_t cs, int ncopy,
-                            double *const *dst, const double *const *src, const size_t *count) {
+// group whose fragment has dst as its Calpha address.  Several plans over
+// one set of buffers run in turn: the first call waits for the allocation
+// (wait_alloc), the later ones queue their copies behind its copies.
+int split_plan_execute_host(SplitPlan *P, cudaStream_t s, const cudaStream_t *cs, int ncs,
+                            int ncopy, double *const *dst, const double *const *src,
+                            const size_t *count, bool wait_alloc) {
   struct Events {
-    cudaEvent_t e[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> e;
     ~Events() {
-      for (auto &x : e)
-        if (x) cudaEventDestroy(x);
+      for (auto x : e) cudaEventDestroy(x);
     }
   } ev;
-  for (auto &x : ev.e) RIMP2_CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+  auto event = [&](cudaEvent_t *out) -> int {
+    RIMP2_CK(cudaEventCreateWithFlags(out, cudaEventDisableTiming));
+    ev.e.push_back(*out);
+    return RIMP2_OK;
+  };
   std::vector<int> owner(ncopy, -1);  // launch group of each copy, -1: none
   size_t bytes[3] = {0, 0, 0};
   int order[3], n = 0;
@@ -3546,25 +3554,36 @@ int split_plan_execute_host(SplitPlan *P, cudaStream_t s, cudaStream_t cs, int n
     if (P->g[k].nfrag) order[n++] = k;
   }
   std::sort(order, order + n, [&](int a, int b) { return bytes[a] < bytes[b]; });
-  // the copy stream starts after the destination buffers' allocation on s
-  RIMP2_CK(cudaEventRecord(ev.e[0], s));
-  RIMP2_CK(cudaStreamWaitEvent(cs, ev.e[0], 0));
-  for (int c = 0; c < ncopy; ++c)
-    if (owner[c] < 0)
-      RIMP2_CK(cudaMemcpyAsync(dst[c], src[c], count[c] * sizeof(double), cudaMemcpyHostToDevice,
-                               cs));
-  RIMP2_CK(cudaEventRecord(ev.e[1], cs));
-  for (int k = 0; k < n; ++k) {
-    for (int c = 0; c < ncopy; ++c)
-      if (owner[c] == order[k])
-        RIMP2_CK(cudaMemcpyAsync(dst[c], src[c], count[c] * sizeof(double),
-                                 cudaMemcpyHostToDevice, cs));
-    RIMP2_CK(cudaEventRecord(ev.e[2 + k], cs));
+  // the copy streams start after the destination buffers' allocation on s
+  // (wait_alloc false: an earlier call on these streams already waited)
+  if (wait_alloc) {
+    cudaEvent_t e0;
+    RIMP2_TRY(event(&e0));
+    RIMP2_CK(cudaEventRecord(e0, s));
+    for (int q = 0; q < ncs; ++q) RIMP2_CK(cudaStreamWaitEvent(cs[q], e0, 0));
   }
-  RIMP2_CK(cudaStreamWaitEvent(s, ev.e[1], 0));
+  // phase 0: copies outside the split groups; phase 1 + k: group order[k]
+  std::vector<cudaEvent_t> done((size_t)(1 + n) * ncs);
+  for (int ph = 0; ph <= n; ++ph) {
+    const int want = ph == 0 ? -1 : order[ph - 1];
+    std::vector<size_t> load(ncs, 0);
+    for (int c = 0; c < ncopy; ++c) {
+      if (owner[c] != want) continue;
+      const int q = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      load[q] += count[c];
+      RIMP2_CK(cudaMemcpyAsync(dst[c], src[c], count[c] * sizeof(double), cudaMemcpyHostToDevice,
+                               cs[q]));
+    }
+    for (int q = 0; q < ncs; ++q) {
+      RIMP2_TRY(event(&done[(size_t)ph * ncs + q]));
+      RIMP2_CK(cudaEventRecord(done[(size_t)ph * ncs + q], cs[q]));
+    }
+  }
+  for (int q = 0; q < ncs; ++q) RIMP2_CK(cudaStreamWaitEvent(s, done[q], 0));
   RIMP2_TRY(plain_plan_record(P->plain, s));
   for (int k = 0; k < n; ++k) {
-    RIMP2_CK(cudaStreamWaitEvent(s, ev.e[2 + k], 0));
+    for (int q = 0; q < ncs; ++q)
+      RIMP2_CK(cudaStreamWaitEvent(s, done[(size_t)(1 + k) * ncs + q], 0));
     RIMP2_TRY(record_group(P->g[order[k]], s, P->nsm, nullptr));
   }
   return RIMP2_OK;

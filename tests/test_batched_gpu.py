@@ -141,11 +141,15 @@ def test_energy_batched_packed_pinned(prec, tol):
     kernels waiting for its own fragments).  Split form: every launch group
     present -- paired kernel (the kernel table set to nocc >= 10, NBA >= 1024
     here), one-CTA kernel with one and with two residual slices, and plain
-    FP64 (nocc * nvirt < 64); FP64 form: all in the plain launch."""
+    FP64 (nocc * nvirt < 64); FP64 form: all in the plain launch.  The two
+    paired-kernel fragments fall in different plans (the host call divides
+    that group by volume so that its first half starts while the second half
+    is copied)."""
     import os
     import torch
     from rimp2_gpu_gb300 import api, autotune
-    shapes = [(12, 256, 1024), (11, 200, 300), (5, 130, 777), (8, 64, 256), (2, 20, 100)]
+    shapes = [(12, 256, 1024), (11, 200, 300), (5, 130, 777), (8, 64, 256), (2, 20, 100),
+              (10, 192, 1024)]
     data = [O.gen_fragment(900 + k, *s) for k, s in enumerate(shapes)]
     ref = [O.pair_energies(v, n, b, Ca, eo, ev, blocked=True)
            for (n, v, b), (Ca, eo, ev) in zip(shapes, data)]
@@ -158,7 +162,8 @@ def test_energy_batched_packed_pinned(prec, tol):
     ev = np.concatenate([d[2] for d in data])
     api.set_split_kernel_rule([0], [10], [1024])
     try:
-        assert [api.split_nslices(v, n, b) for n, v, b in shapes] == [1, 1, 1, 2, 0]
+        assert [api.split_nslices(v, n, b) for n, v, b in shapes] == [1, 1, 1, 2, 0, 1]
+        assert [api.split_kernel_for(v, n, b) for n, v, b in shapes] == [2, 1, 1, 1, 0, 2]
         res = api.energy_batched_packed([s[0] for s in shapes], [s[1] for s in shapes],
                                         [s[2] for s in shapes], cav, eo, ev, precision=prec)
     finally:
