@@ -1339,6 +1339,9 @@ int rimp2_energy_batched(const int *nfrag, const int *nocc, const int *nvirt, co
                                      pd[p].data(), ps[p].data(), pn[p].data(), !waited);
         waited = true;
       }
+    // after a failure some copies may still be in flight on the copy stream,
+    // not ordered before the buffers' release on s: let them finish first
+    if (rc != RIMP2_OK) cudaStreamSynchronize(cs);
     for (auto pl : plans)  // keeps the error message of a failed execute
       if (pl) split_plan_destroy((SplitPlan *)pl);
     RIMP2_TRY(rc);
