@@ -84,8 +84,6 @@ def parse():
                     help="batched workload: the first N of the 256 seeded shapes (profiling)")
     ap.add_argument("--ao-fragments", type=int, default=AO_N_DEFAULT,
                     help="fragments in the AO pipeline workload")
-    ap.add_argument("--ao-serial", action="store_true",
-                    help="AO pipeline: run the metric Cholesky after the transform, not beside it")
     ap.add_argument("--ao-transform", choices=["split", "fp64"], default="split",
                     help="AO->MO transform on the tensor cores (split) or in FP64; the metric "
                          "Cholesky and the triangular solve are FP64 either way")
@@ -830,25 +828,32 @@ def mo_coefficients(nbas, seed):
     return np.asfortranarray(q * np.sign(np.diag(r)))
 
 
-def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None, serial=False):
-    """Config 5: per fragment the AO tensor is generated on the device (untimed
-    input creation), then Calpha is formed on the GPU (AO->MO transform,
-    metric Cholesky, triangular solve; timed), and finally all fragments'
-    energies run as one graph-launched batched split-precision launch (timed).
+def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
+    """Config 5: the AO tensors are generated on the device (untimed input
+    creation, two fragments at a time), then Calpha is formed on the GPU
+    (AO->MO transform, metric Cholesky, triangular solve; timed), and finally
+    all fragments' energies run as one graph-launched batched split-precision
+    launch (timed).  The two fragments of a pair run as a pipeline on three
+    streams: the first fragment's transform beside its Cholesky (the
+    critical path), then its FP64 solve, during which the second fragment's
+    transform and Cholesky run, then the second solve.
     check "full"/"sample": every 16th fragment (at least one) against the GPU
     FP64 energy kernel."""
-    st = torch.cuda.Stream(device=dev)
-    # metric Cholesky, concurrent with the transform; high priority so that its
-    # latency-bound diagonal-block chain gets SMs ahead of the transform's CTAs
+    st = torch.cuda.Stream(device=dev)  # solves, and the step's bracket
+    stt = torch.cuda.Stream(device=dev)  # AO->MO transforms
+    # metric Cholesky: high priority so that its latency-bound diagonal-block
+    # chain gets SMs ahead of the transform's and the solve's CTAs
     st2 = torch.cuda.Stream(device=dev, priority=-1)
     sp = st.cuda_stream
     maxao = max(b * b * nba for b, nba, _, _ in shapes)
     maxv = max(nba * nba for _, nba, _, _ in shapes)
     maxb = max(nba * nvirt * nocc for _, nba, nocc, nvirt in shapes)
+    npipe = min(2, len(shapes))  # fragments whose inputs are resident together
     with torch.cuda.stream(st):
-        ao = torch.empty(maxao, dtype=torch.float64, device=dev)
-        V = torch.empty(maxv, dtype=torch.float64, device=dev)
-        Bw = torch.empty(maxb, dtype=torch.float64, device=dev)  # (alpha|a i) work array
+        ao = [torch.empty(maxao, dtype=torch.float64, device=dev) for _ in range(npipe)]
+        V = [torch.empty(maxv, dtype=torch.float64, device=dev) for _ in range(npipe)]
+        # (alpha|a i) work arrays
+        Bw = [torch.empty(maxb, dtype=torch.float64, device=dev) for _ in range(npipe)]
     frags, desc = [], []
     for f, (nbas, nba, nocc, nvirt) in enumerate(shapes):
         with torch.cuda.stream(st):
@@ -879,36 +884,51 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None, se
     eff = sum(2.0 * nba * (nocc * nvirt) ** 2 for _, nba, nocc, nvirt in shapes)
     n0 = None
     parts_ms = []
+    ev_t = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     for step in range(warmup + steps):
         if step == warmup:
             n0 = api.kernel_launch_count()
         fe = 0.0
         tr = ch = so = win = 0.0
-        for f, (nbas, nba, nocc, nvirt) in enumerate(shapes):
-            api.gen_ao_dev(4000 + f, nba, nbas, ao.data_ptr(), V.data_ptr(), stream=sp)
+        for g0 in range(0, len(shapes), npipe):
+            grp = list(range(g0, min(g0 + npipe, len(shapes))))
+            for k, f in enumerate(grp):
+                nbas, nba, _, _ = shapes[f]
+                api.gen_ao_dev(4000 + f, nba, nbas, ao[k].data_ptr(), V[k].data_ptr(), stream=sp)
             st.synchronize()  # inputs complete before the timed section
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
-            # the AO->MO transform (tensor cores, HBM) and the metric Cholesky
-            # (FP64, latency-bound diagonal chain) are independent: they run
-            # concurrently on two streams; the triangular solve joins them
-            ev[0].record(st)
-            api.ao2mo_dev(nba, nbas, nocc, nvirt, ao.data_ptr(), frags[f]["Cmo"].data_ptr(),
-                          Bw.data_ptr(), split=(transform == "split"), stream=sp)
-            ev[1].record(st)
-            st2.wait_event(ev[1] if serial else ev[0])  # serial: the Cholesky after the transform
-            api.cholesky_dev(nba, V.data_ptr(), stream=st2.cuda_stream)
-            ev[3].record(st2)
-            st.wait_stream(st2)
-            ev[4].record(st)
-            api.trsm_lower_dev(nba, nvirt * nocc, V.data_ptr(), Bw.data_ptr(),
-                               frags[f]["C"].data_ptr(), stream=sp)
-            ev[5].record(st)
+            t0 = ev_t()
+            t0.record(st)
+            stt.wait_event(t0)
+            st2.wait_event(t0)
+            tA, tB, cA, cB, sA, sB = ([ev_t() for _ in grp] for _ in range(6))
+            for k, f in enumerate(grp):
+                nbas, nba, nocc, nvirt = shapes[f]
+                # a later fragment's transform waits for the earlier Cholesky,
+                # so that it runs beside the earlier solve, off the critical path
+                if k > 0:
+                    stt.wait_event(cB[k - 1])
+                tA[k].record(stt)
+                api.ao2mo_dev(nba, nbas, nocc, nvirt, ao[k].data_ptr(), frags[f]["Cmo"].data_ptr(),
+                              Bw[k].data_ptr(), split=(transform == "split"),
+                              stream=stt.cuda_stream)
+                tB[k].record(stt)
+                cA[k].record(st2)
+                # returns when the factorisation is done (it reads the pivot
+                # check back), so the solve is enqueued right after it
+                api.cholesky_dev(nba, V[k].data_ptr(), stream=st2.cuda_stream)
+                cB[k].record(st2)
+                st.wait_event(tB[k])
+                st.wait_event(cB[k])
+                sA[k].record(st)
+                api.trsm_lower_dev(nba, nvirt * nocc, V[k].data_ptr(), Bw[k].data_ptr(),
+                                   frags[f]["C"].data_ptr(), stream=sp)
+                sB[k].record(st)
             st.synchronize()
-            tr += ev[0].elapsed_time(ev[1])
-            ch += ev[0].elapsed_time(ev[3])
-            so += ev[4].elapsed_time(ev[5])
-            win += ev[0].elapsed_time(ev[4])
-            fe += ev[0].elapsed_time(ev[5])
+            tr += sum(a.elapsed_time(b) for a, b in zip(tA, tB))
+            ch += sum(a.elapsed_time(b) for a, b in zip(cA, cB))
+            so += sum(a.elapsed_time(b) for a, b in zip(sA, sB))
+            win += t0.elapsed_time(sA[0])
+            fe += t0.elapsed_time(sB[-1])
         if step >= warmup:
             parts_ms.append((tr, ch, so, win))
         if plan is None:
@@ -927,24 +947,25 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None, se
     # the transform alone (no Cholesky beside it), on the last fragment's AO
     # tensor, still in place; the tensor exceeds L2, so every run reads HBM
     nbas_l, nba_l, nocc_l, nvirt_l = shapes[-1]
+    kl = (len(shapes) - 1) % npipe  # the buffers that hold the last fragment
     alone = []
     for _ in range(3):
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record(st)
-        api.ao2mo_dev(nba_l, nbas_l, nocc_l, nvirt_l, ao.data_ptr(), frags[-1]["Cmo"].data_ptr(),
-                      Bw.data_ptr(), split=(transform == "split"), stream=sp)
+        api.ao2mo_dev(nba_l, nbas_l, nocc_l, nvirt_l, ao[kl].data_ptr(), frags[-1]["Cmo"].data_ptr(),
+                      Bw[kl].data_ptr(), split=(transform == "split"), stream=sp)
         a1.record(st)
         st.synchronize()
         alone.append(a0.elapsed_time(a1))
     alone_ms = statistics.median(alone[1:])
     # the Cholesky alone, on the last fragment's metric generated afresh
-    api.gen_ao_dev(4000 + len(shapes) - 1, nba_l, nbas_l, 0, V.data_ptr(), stream=sp)
+    api.gen_ao_dev(4000 + len(shapes) - 1, nba_l, nbas_l, 0, V[kl].data_ptr(), stream=sp)
     st.synchronize()
     c0 = torch.cuda.Event(enable_timing=True)
     c1 = torch.cuda.Event(enable_timing=True)
     c0.record(st)
-    api.cholesky_dev(nba_l, V.data_ptr(), stream=sp)
+    api.cholesky_dev(nba_l, V[kl].data_ptr(), stream=sp)
     c1.record(st)
     st.synchronize()
     chol_alone_ms = c0.elapsed_time(c1)
@@ -984,9 +1005,10 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None, se
     return {"value": eff / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms,
             "fragments": len(shapes), "shapes_nbas_nba_nocc_nvirt": [list(x) for x in shapes[:4]],
             "ao_transform": transform, "front_end_ms": fe_m, "energy_ms": en_m,
-            "front_end_overlap": ("metric Cholesky after the AO->MO transform" if serial else
-                                  "AO->MO transform and metric Cholesky run concurrently "
-                                  "(two streams); parts overlap"),
+            "front_end_overlap": "per pair of fragments: transform beside Cholesky, the second "
+                                 "fragment's transform and Cholesky beside the first solve "
+                                 "(three streams); the parts overlap, front_end_ms is the "
+                                 "pipeline's span",
             "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,
             "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
             "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
@@ -1020,7 +1042,7 @@ def run_ao(args):
         b = args.ao_nbas
         shapes = [(b, 3 * b, b // 10, b - b // 10)] * len(shapes)
     r = ao_leg(api, torch, dev, shapes, args.steps, args.warmup, args.ao_transform, args.check,
-               pg=pg, serial=args.ao_serial)
+               pg=pg)
     if rank == 0:
         cfg = {k: v for k, v in r.items() if k not in ("value", "unit", "ms_per_step",
                                                        "accuracy", "gpu_launches")}
