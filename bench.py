@@ -830,13 +830,13 @@ def mo_coefficients(nbas, seed):
 
 def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
     """Config 5: the AO tensors are generated on the device (untimed input
-    creation, two fragments at a time), then Calpha is formed on the GPU
-    (AO->MO transform, metric Cholesky, triangular solve; timed), and finally
-    all fragments' energies run as one graph-launched batched split-precision
-    launch (timed).  The two fragments of a pair run as a pipeline on three
-    streams: the first fragment's transform beside its Cholesky (the
-    critical path), then its FP64 solve, during which the second fragment's
-    transform and Cholesky run, then the second solve.
+    creation, up to four fragments at a time), then Calpha is formed on the
+    GPU (AO->MO transform, metric Cholesky, triangular solve; timed), and
+    finally all fragments' energies run as one graph-launched batched
+    split-precision launch (timed).  The fragments of a group run as a
+    pipeline on three streams: the first fragment's transform beside its
+    Cholesky (the critical path), then its FP64 solve, during which the next
+    fragment's transform and Cholesky run, and so on.
     check "full"/"sample": every 16th fragment (at least one) against the GPU
     FP64 energy kernel."""
     st = torch.cuda.Stream(device=dev)  # solves, and the step's bracket
@@ -848,7 +848,7 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
     maxao = max(b * b * nba for b, nba, _, _ in shapes)
     maxv = max(nba * nba for _, nba, _, _ in shapes)
     maxb = max(nba * nvirt * nocc for _, nba, nocc, nvirt in shapes)
-    npipe = min(2, len(shapes))  # fragments whose inputs are resident together
+    npipe = min(4, len(shapes))  # fragments whose inputs are resident together
     with torch.cuda.stream(st):
         ao = [torch.empty(maxao, dtype=torch.float64, device=dev) for _ in range(npipe)]
         V = [torch.empty(maxv, dtype=torch.float64, device=dev) for _ in range(npipe)]
@@ -1005,10 +1005,10 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
     return {"value": eff / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms,
             "fragments": len(shapes), "shapes_nbas_nba_nocc_nvirt": [list(x) for x in shapes[:4]],
             "ao_transform": transform, "front_end_ms": fe_m, "energy_ms": en_m,
-            "front_end_overlap": "per pair of fragments: transform beside Cholesky, the second "
-                                 "fragment's transform and Cholesky beside the first solve "
-                                 "(three streams); the parts overlap, front_end_ms is the "
-                                 "pipeline's span",
+            "front_end_overlap": "per group of up to four fragments: transform beside "
+                                 "Cholesky, the next fragment's transform and Cholesky beside "
+                                 "the current solve (three streams); the parts overlap, "
+                                 "front_end_ms is the pipeline's span",
             "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,
             "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
             "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
