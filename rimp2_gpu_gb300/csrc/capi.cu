@@ -138,6 +138,13 @@ cudaStream_t copy_stream() {
   return g_copy_stream;
 }
 
+static cudaStream_t g_slice_stream = nullptr;
+cudaStream_t slice_stream() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_slice_stream) cudaStreamCreateWithFlags(&g_slice_stream, cudaStreamNonBlocking);
+  return g_slice_stream;
+}
+
 
 }  // namespace rimp2
 

@@ -155,6 +155,7 @@ int rcp_denom_selftest(int n, const float *d, float *r, float *ref, cudaStream_t
 int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs &a,
                           cudaStream_t s, cudaStream_t copy_s, int chunk_occ);
 cudaStream_t copy_stream();
+cudaStream_t slice_stream();  // the streamed host path's slicing
 // K-major FP16 slices of a set of rows (split GEMM operand)
 struct SlicedOp {
   int nsl = 2, nks = 0;

@@ -3624,8 +3624,10 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   // Occupied-index chunk boundaries: the first chunk small (its copy is the
   // only one nothing hides), later ones growing by half, since chunk c's
   // work grows with its column indices j while its copy does not; chunk_occ
-  // caps the first chunk.  The energy of chunk c starts as soon as its copy
-  // lands, so after the first few chunks the copy engine runs ahead.
+  // caps the first chunk.  Chunk c is sliced on the slicing stream as soon
+  // as its copy lands, beside chunk c-1's energy kernel, and its energy
+  // kernel starts once it is sliced, so after the first few chunks the copy
+  // engine and the slicer run ahead of the tensor cores.
   std::vector<int> bnd;
   for (int b = std::min(a.nocc, std::max(1, std::min(chunk_occ, 4))); ;) {
     bnd.push_back(b);
@@ -3646,12 +3648,19 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   const FragDesc *fr = g.frags.as<FragDesc>();
   int rc = RIMP2_OK;
   const int nchunk = (int)bnd.size();
-  std::vector<cudaEvent_t> ev(nchunk, nullptr);
+  // ev[c]: chunk c copied (copy stream); ev[nchunk + c]: chunk c sliced
+  // (slicing stream); ev[2 nchunk]: the plan's buffers exist (stream s)
+  std::vector<cudaEvent_t> ev(2 * nchunk + 1, nullptr);
   for (auto &e : ev)
     if (rc == RIMP2_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
       set_error("event creation failed");
       rc = RIMP2_ERR_CUDA;
     }
+  cudaStream_t ss = slice_stream();
+  if (rc == RIMP2_OK && !ss) {
+    set_error("slicing stream unavailable");
+    rc = RIMP2_ERR_CUDA;
+  }
   const size_t slab = (size_t)a.NBA * a.nvirt;  // doubles per occupied index
   // copies first, so the copy engine runs ahead of the compute stream
   for (int c = 0; c < nchunk && rc == RIMP2_OK; ++c) {
@@ -3669,6 +3678,29 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
     eps_batch_kernel<<<g2, 256, 0, s>>>(fr, g.eo2.as<float2>(), g.ev2.as<float2>());
     count_launch(1);
   }
+  // slicing of every chunk on the slicing stream, each after its copy (and
+  // after the plan's buffers, allocated on s); columns of different chunks
+  // are disjoint in the slices, scales and corrections
+  if (rc == RIMP2_OK) {
+    cudaError_t e = cudaEventRecord(ev[2 * nchunk], s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ss, ev[2 * nchunk], 0);
+    for (int c = 0; c < nchunk && e == cudaSuccess; ++c) {
+      const int i0 = c ? bnd[c - 1] : 0, i1 = bnd[c];
+      const int col0 = i0 * F.nvpad, col1 = i1 * F.nvpad;
+      e = cudaStreamWaitEvent(ss, ev[c], 0);
+      if (e != cudaSuccess) break;
+      slice_batch_kernel<<<(unsigned)(((long long)(col1 - col0) * 32 + 255) / 256), 256, 0, ss>>>(
+          fr, g.nsl, g.R * 64, g.slices.as<__half>(), g.inv.as<float>(), col0, col1,
+          g.pair ? 1 : 0, g.dcorr.as<float>());
+      count_launch(1);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaEventRecord(ev[nchunk + c], ss);
+    }
+    if (e != cudaSuccess) {
+      set_error("streamed slicing failed: %s", cudaGetErrorString(e));
+      rc = RIMP2_ERR_CUDA;
+    }
+  }
   BatchParams BP;
   BP.frags = fr;
   BP.items = g.items.as<int4>();
@@ -3679,17 +3711,12 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   BP.err = device_error_word();
   for (int c = 0; c < nchunk && rc == RIMP2_OK; ++c) {
     const int i0 = c ? bnd[c - 1] : 0, i1 = bnd[c];
-    cudaError_t e = cudaStreamWaitEvent(s, ev[c], 0);
+    cudaError_t e = cudaStreamWaitEvent(s, ev[nchunk + c], 0);
     if (e != cudaSuccess) {
       set_error("stream wait failed: %s", cudaGetErrorString(e));
       rc = RIMP2_ERR_CUDA;
       break;
     }
-    const int col0 = i0 * F.nvpad, col1 = i1 * F.nvpad;
-    slice_batch_kernel<<<(unsigned)(((long long)(col1 - col0) * 32 + 255) / 256), 256, 0, s>>>(
-        fr, g.nsl, g.R * 64, g.slices.as<__half>(), g.inv.as<float>(), col0, col1,
-        g.pair ? 1 : 0, g.dcorr.as<float>());
-    count_launch(1);
     e = cudaMemsetAsync(g.queue.p, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) {
       set_error("queue reset failed: %s", cudaGetErrorString(e));
@@ -3722,10 +3749,17 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
       BP.queue = g.queue.as<unsigned int>();
       const int grid = (int)std::min<long long>(BP.nitems - BP.item_begin, P->nsm);
       note_split_kernel(1);
+      // at the highest priority, like the paired kernel: the next chunk's
+      // slicing blocks wait behind this kernel's CTAs, not ahead of them
       if (g.nsl == 2)
-        split_batch_kernel<2, 3><<<grid, BATCH_THREADS, smem_bytes(2, 3), s>>>(g.tm, BP);
+        e = launch_hi(split_batch_kernel<2, 3>, grid, BATCH_THREADS, smem_bytes(2, 3), s, g.tm, BP);
       else
-        split_batch_kernel<3, 2><<<grid, BATCH_THREADS, smem_bytes(3, 2), s>>>(g.tm, BP);
+        e = launch_hi(split_batch_kernel<3, 2>, grid, BATCH_THREADS, smem_bytes(3, 2), s, g.tm, BP);
+      if (e != cudaSuccess) {
+        set_error("split launch failed: %s", cudaGetErrorString(e));
+        rc = RIMP2_ERR_CUDA;
+        break;
+      }
     }
     count_launch(1);
     e = cudaGetLastError();
@@ -3749,6 +3783,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   // the caller can release dCa
   if (rc != RIMP2_OK) {
     cudaStreamSynchronize(copy_s);
+    if (ss) cudaStreamSynchronize(ss);
     cudaStreamSynchronize(s);
   }
   for (auto &e : ev)
