@@ -3338,18 +3338,26 @@ struct SplitPlan {
 
 bool split_supported() { return get_encode() != nullptr; }
 
-// Records the launch groups of a plan.  With two or more groups, every
-// group's inputs (slicing, orbital-energy pairs) go on a side branch, in the
-// order the energy kernels run, and each energy kernel waits only for its
-// own group's inputs: the slicing of the next group runs while the current
-// group's persistent kernel holds the SMs (a slicing block fits beside an
-// energy CTA), instead of between the two kernels.  The group with the least
-// slicing work goes first, since nothing hides its inputs.
+// Records the launch groups of a plan, one after the other (slicing, then
+// the energy kernel and reductions of each group).  The overlapped form
+// (RIMP2_BATCH_OVERLAP=1): with two or more groups, every group's inputs
+// (slicing, orbital-energy pairs) go on a side branch, in the order the
+// energy kernels run, and each energy kernel waits only for its own group's
+// inputs, so the slicing of the next group runs while the current group's
+// persistent kernel holds the SMs (a slicing block fits beside an energy
+// CTA); the group with the least slicing work goes first, since nothing
+// hides its inputs.
 int record_plan_overlapped(SplitPlan *P, cudaStream_t s) {
   int order[3], n = 0;
   for (int k = 0; k < 3; ++k)
     if (P->g[k].nfrag) order[n++] = k;
-  if (n < 2) {
+  // measured on GB300 (256-fragment batch, same box, alternating runs):
+  // 633.9 / 635.4 eff TFLOP/s with the groups one after the other against
+  // 626.9 / 631.1 with the side branch -- under the power cap the slicing
+  // beside an energy kernel costs that kernel more than it hides.  So the
+  // groups run in sequence unless RIMP2_BATCH_OVERLAP=1.
+  const char *ov = getenv("RIMP2_BATCH_OVERLAP");
+  if (n < 2 || !(ov && ov[0] == '1')) {
     for (int k = 0; k < n; ++k) RIMP2_TRY(record_group(P->g[order[k]], s, P->nsm, nullptr));
     return RIMP2_OK;
   }
@@ -3656,7 +3664,9 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
       set_error("event creation failed");
       rc = RIMP2_ERR_CUDA;
     }
-  cudaStream_t ss = slice_stream();
+  // RIMP2_STREAM_SLICE=0: slice on s, between the energy launches
+  const char *sv = getenv("RIMP2_STREAM_SLICE");
+  cudaStream_t ss = (sv && sv[0] == '0') ? s : slice_stream();
   if (rc == RIMP2_OK && !ss) {
     set_error("slicing stream unavailable");
     rc = RIMP2_ERR_CUDA;
@@ -3783,7 +3793,7 @@ int split_energy_streamed(const double *hCa, double *dCa, const SplitEnergyArgs 
   // the caller can release dCa
   if (rc != RIMP2_OK) {
     cudaStreamSynchronize(copy_s);
-    if (ss) cudaStreamSynchronize(ss);
+    if (ss && ss != s) cudaStreamSynchronize(ss);
     cudaStreamSynchronize(s);
   }
   for (auto &e : ev)
