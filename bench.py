@@ -1010,6 +1010,9 @@ def ao_leg(api, torch, dev, shapes, steps, warmup, transform, check, pg=None):
                                  "the current solve (three streams); the parts overlap, "
                                  "front_end_ms is the pipeline's span",
             "transform_ms": tr_m, "cholesky_ms": ch_m, "solve_ms": so_m,
+            "parts_note": "transform_ms, cholesky_ms and solve_ms (and the rates from them) are "
+                          "each part's own span inside the pipeline, where the parts share the "
+                          "GPU; transform_alone and cholesky_alone time them by themselves",
             "transform_tflops": tr_flop / (tr_m * 1e-3) / 1e12,
             "transform_algorithmic_gbs": ao_bytes / (tr_m * 1e-3) / 1e9,
             "transform_algorithmic_bytes": ao_bytes,
