@@ -175,3 +175,32 @@ def test_energy_batched_packed_pinned(prec, tol):
     with pytest.raises(ValueError):
         api.energy_batched_packed([s[0] for s in shapes], [s[1] for s in shapes],
                                   [s[2] for s in shapes], cav[:-1], eo, ev, precision=prec)
+
+
+def test_batch_graph_overlap_forms_bitwise(frags, monkeypatch):
+    """The batch graph with the launch groups in sequence (default) and with
+    the next group's slicing on a side branch (RIMP2_BATCH_OVERLAP=1) runs
+    the same kernels on the same items: the energies agree bit for bit."""
+    import torch
+    from rimp2_gpu_gb300 import api
+    out = []
+    for ov in ("0", "1"):
+        monkeypatch.setenv("RIMP2_BATCH_OVERLAP", ov)
+        dev = []
+        for Ca, eo, ev, _, _ in frags:
+            nocc, nvirt, NBA = eo.size, ev.size, Ca.shape[0]
+            dev.append((nocc, nvirt, NBA, dict(
+                C=torch.from_numpy(Ca.ravel(order="F")).cuda(), eo=torch.from_numpy(eo).cuda(),
+                ev=torch.from_numpy(ev).cuda(),
+                E=torch.zeros(nocc * nocc, dtype=torch.float64, device="cuda"),
+                T=torch.zeros(1, dtype=torch.float64, device="cuda"))))
+        desc = [(n, v, b, t["C"].data_ptr(), t["eo"].data_ptr(), t["ev"].data_ptr(),
+                 t["E"].data_ptr(), t["T"].data_ptr()) for n, v, b, t in dev]
+        plan = api.BatchPlan(desc, nslices=[0, 1, 2, 0, 1, 0], graph=True)
+        plan.execute()
+        torch.cuda.synchronize()
+        api.sync_status()
+        plan.close()
+        out.append([(t["E"].cpu().numpy(), t["T"].item()) for _, _, _, t in dev])
+    for (a, ta), (b, tb) in zip(*out):
+        assert np.array_equal(a, b) and ta == tb

@@ -268,6 +268,25 @@ def test_pair_kernel_host_streamed(api, kernel_choice, nocc, nvirt, NBA):
     assert abs(E - Er) <= 1e-7 * abs(Er)
 
 
+@pytest.mark.parametrize("pair", ["0", "1"])
+def test_streamed_slicing_placement_bitwise(api, kernel_choice, monkeypatch, pair):
+    """The host call slices each occupied chunk on its own stream beside the
+    previous chunk's energy kernel; with RIMP2_STREAM_SLICE=0 it slices on
+    the energy stream between the launches.  The same kernels compute the
+    same items and reduce them in the same order: the energies must agree
+    bit for bit, and with the oracle within 1e-7."""
+    nocc, nvirt, NBA = 40, 200, 640  # seven chunks: 4, 6, 9, 13, 19, 28, 40 occupied indices
+    Ca, eo, ev = O.gen_fragment(880, nocc, nvirt, NBA)
+    Epr, Er = O.pair_energies(nvirt, nocc, NBA, Ca, eo, ev, blocked=True)
+    kernel_choice(pair)
+    Ep1, E1 = api.energy(nvirt, nocc, NBA, Ca, eo, ev, precision=api.PREC_SPLIT)
+    monkeypatch.setenv("RIMP2_STREAM_SLICE", "0")
+    Ep0, E0 = api.energy(nvirt, nocc, NBA, Ca, eo, ev, precision=api.PREC_SPLIT)
+    assert np.array_equal(Ep1, Ep0) and E1 == E0
+    assert (np.abs(Ep1 - Epr) / np.abs(Epr)).max() <= 1e-7
+    assert abs(E1 - Er) <= 1e-7 * abs(Er)
+
+
 def test_pair_kernel_long_K_against_oracle(api, kernel_choice):
     """A long auxiliary space on the paired-CTA kernel (one residual slice,
     forced: the kernel table starts it at nocc >= 16 for this bucket):
