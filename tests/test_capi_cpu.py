@@ -48,6 +48,25 @@ def test_argument_validation_before_device():
     assert b"bad dims" in _lib.lib().rimp2_last_error_string()
 
 
+def test_batched_packed_input_validation():
+    """The packed batched call checks its packing on the host (sizes against
+    the fragment dimensions) and the library checks the dimensions before it
+    touches a device."""
+    from rimp2_gpu_gb300 import api, _lib
+    nocc, nvirt, nba = [2, 3], [4, 5], [6, 7]
+    ca = np.zeros(2 * 4 * 6 + 3 * 5 * 7)
+    eo, ev = np.zeros(5), np.zeros(9)
+    with pytest.raises(ValueError):
+        api.energy_batched_packed(nocc, nvirt, nba, ca[:-1], eo, ev)
+    with pytest.raises(ValueError):
+        api.energy_batched_packed(nocc, nvirt, nba, ca, eo[:-1], ev)
+    with pytest.raises(ValueError):
+        api.energy_batched_packed(nocc, nvirt[:1], nba, ca, eo, ev)
+    with pytest.raises(_lib.Rimp2Error) as ei:  # zero dimension: status 1 before the device
+        api.energy_batched_packed([2, 0], [4, 5], [6, 7], np.zeros(48), np.zeros(2), np.zeros(9))
+    assert ei.value.status == 1 and "bad dims" in str(ei.value)
+
+
 @pytest.mark.skipif(has_gpu(), reason="checks the no-GPU status path")
 def test_no_gpu_reports_status_not_fallback():
     from rimp2_gpu_gb300 import api, _lib
