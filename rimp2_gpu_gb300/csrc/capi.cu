@@ -145,7 +145,6 @@ cudaStream_t slice_stream() {
   return g_slice_stream;
 }
 
-
 }  // namespace rimp2
 
 using namespace rimp2;
