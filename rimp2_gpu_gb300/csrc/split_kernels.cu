@@ -3529,8 +3529,9 @@ void split_plan_destroy(SplitPlan *P) { delete P; }
 // copy streams cs[0..ncs) launch group by launch group, the group with the
 // least Calpha first; copies that belong to no split group (orbital
 // energies, the plain FP64 fragments) go before all of them.  Within a
-// group each copy goes to the stream with the fewest bytes so far, so that
-// several copy engines share the transfer.  Each group's slicing waits only
+// group each copy goes to the stream with the fewest bytes so far (the
+// batched host call passes one stream: four were measured slower).  Each
+// group's slicing waits only
 // for its own fragments' copies, so the transfer of the later, larger
 // groups overlaps the kernels of the earlier ones.  A copy belongs to the
 // group whose fragment has dst as its Calpha address.  Several plans over
@@ -3596,7 +3597,6 @@ int split_plan_execute_host(SplitPlan *P, cudaStream_t s, const cudaStream_t *cs
   }
   return RIMP2_OK;
 }
-
 
 int bounded_wait_selftest(long long budget_cycles, cudaStream_t s) {
   wait_selftest_kernel<<<1, 32, 0, s>>>(budget_cycles, device_error_word());
